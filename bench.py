@@ -1,0 +1,441 @@
+"""Benchmark of the GB300 PIC deposition path.
+
+Workload (the deposition benchmark shape): 1024x1024 periodic grid, dx = 1,
+64 particles per cell = 67,108,864 particles, x drawn from density
+1 + 0.01*cos(2*pi*x/1024) by rejection sampling, y uniform, Maxwellian
+velocities vth = 0.1, charge -1, seeded synthetic data. The particles are
+cell-sorted once before timing.
+
+One step = one CIC charge deposition of all particles into an FP64 rho grid
+(clear + tiled fixed-point deposit + conversion), particles resident in HBM.
+The particle stream (1.07 GB) is far larger than L2 (129 MB), so no L2 flush is
+needed between steps.
+
+  value   particles/s over the timed steps (CUDA events on the library stream),
+          summed over ranks (replicas; one GPU each), max time over ranks.
+  e2e     the same metric through the public C ABI with host buffers: every
+          step uploads x, y, q (FP64, pinned) and downloads rho (FP64).
+  roofline  the deposit kernel alone: algorithmic bytes (16 B per particle +
+          8 B per cell) / its mean CUDA-event duration, against the measured
+          HBM copy bandwidth in MEASURED_PEAKS.json.
+  cpu_baseline  the reference's FP64 CPU deposit on the host cores (rank 0).
+
+--impl reference times the reference's own CPU path (oracle/_ref when it loads
+on this machine, else the oracle's C restatement of it) on the same workload,
+per step a bounded slice of it, with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "pic-deposition_gb300"))
+
+NX = NY = 1024
+PPC = 64
+AMP = 0.01
+VTH = 0.1
+ESK_DT = 0.1
+SCHEMES = {"NGP": 0, "CIC": 1, "TSC": 2, "Esirkepov": 3}
+BYTES_PER_PARTICLE = 16  # x_rel, y_rel, q (FP32) + cell key (u32)
+BYTES_PER_PARTICLE_ESK = 24  # + vx, vy
+BYTES_PER_CELL = 8  # int64 rho written once
+METRIC = "deposit particles/s (CIC, 64M cell-sorted particles, 1024x1024)"
+WORKLOAD = "cic_deposit_1024x1024_64ppc_sorted"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """dram bytes per deposit launch from the committed ncu summary (None if absent)."""
+    path = os.path.join(ROOT, "profiles", "deposit_tiled_cic_1024x1024_64ppc.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                try:
+                    return float(line.split(":", 1)[1].split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+class CudaEvents:
+    """CUDA events on a raw stream handle (libcudart via ctypes)."""
+
+    def __init__(self):
+        for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+            try:
+                self.rt = C.CDLL(name)
+                break
+            except OSError:
+                continue
+        rt = self.rt
+        rt.cudaEventCreate.argtypes = [C.POINTER(C.c_void_p)]
+        rt.cudaEventRecord.argtypes = [C.c_void_p, C.c_void_p]
+        rt.cudaEventSynchronize.argtypes = [C.c_void_p]
+        rt.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
+        rt.cudaEventDestroy.argtypes = [C.c_void_p]
+
+    def event(self):
+        e = C.c_void_p()
+        assert self.rt.cudaEventCreate(C.byref(e)) == 0
+        return e
+
+    def record(self, e, stream):
+        assert self.rt.cudaEventRecord(e, C.c_void_p(stream)) == 0
+
+    def elapsed_ms(self, a, b):
+        assert self.rt.cudaEventSynchronize(b) == 0
+        ms = C.c_float()
+        assert self.rt.cudaEventElapsedTime(C.byref(ms), a, b) == 0
+        return float(ms.value)
+
+
+def make_workload(seed: int):
+    import workloads
+
+    return workloads.density_cos(NX, NY, PPC, AMP, VTH, seed=seed)
+
+
+def cpu_deposit_timer(threads: int):
+    """Returns (fn(p) -> seconds for one FP64 CIC deposit, kind)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    kind = "port"
+    ref = None
+    if oracle.Ref.available():
+        try:
+            ref = oracle.Ref()
+            kind = "reference"
+        except OSError:
+            ref = None
+    port = oracle.Port()
+
+    def run(p, scheme=1):
+        if ref is not None:
+            # the reference's own timer: depositChargeTimedSoA (deposition.cpp:257-310), deposit only
+            st = ref.deposit_timed(NX, NY, float(NX), float(NY), scheme, p, dt=ESK_DT, threads=threads, repeats=1)
+            return st["deposit_ms"] / 1e3
+        t0 = time.perf_counter()
+        port.deposit_ref(NX, NY, float(NX), float(NY), scheme, p, dt=ESK_DT, threads=threads)
+        return time.perf_counter() - t0
+
+    return run, kind
+
+
+def sorted_order(p):
+    key = np.floor(p["y"]).astype(np.int64) * NX + np.floor(p["x"]).astype(np.int64)
+    return np.argsort(key, kind="stable")
+
+
+def run_reference(args, d: Dist):
+    out = {"impl": "reference", "metric": METRIC, "unit": "particles/s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic (seeded)"}
+    if d.rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    p = make_workload(42)
+    order = sorted_order(p)
+    p = {k: v[order] for k, v in p.items()}
+    run, kind = cpu_deposit_timer(threads)
+    n = len(p["x"])
+    # size each step's slice so that warmup + steps take about 90 s
+    probe = min(n, 4_000_000)
+    sl = {k: v[:probe] for k, v in p.items()}
+    run(sl)
+    rate = probe / max(run(sl), 1e-6)
+    per_step = int(min(n, max(1_000_000, rate * 90.0 / max(1, args.steps + args.warmup))))
+    sl = {k: v[:per_step] for k, v in p.items()}
+    for _ in range(args.warmup):
+        run(sl)
+    tot = 0.0
+    for _ in range(args.steps):
+        tot += run(sl)
+    value = per_step * args.steps / tot
+    out.update(value=value, ms_per_step=1e3 * tot / args.steps,
+               config={"workload": WORKLOAD, "grid": [NX, NY], "particles": n, "sample_particles_per_step": per_step,
+                       "l2": "inputs larger than L2 not applicable (CPU)"},
+               cpu_baseline={"value": value, "unit": "particles/s", "cores": threads, "kind": kind,
+                             "sample": f"first {per_step} cell-sorted particles of the workload per step, "
+                                       f"FP64 CIC deposit (reference src/deposition/deposition_parallel.cpp "
+                                       f"privatised OpenMP form)"},
+               e2e={"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
+    return out
+
+
+def run_gpu(args, d: Dist):
+    import pic_gb300 as pg
+
+    scheme = SCHEMES[args.scheme]
+    dev = d.local if d.ws > 1 else 0
+    p = make_workload(42 + d.rank)
+    n = len(p["x"])
+    G = NX * NY
+    ev = CudaEvents()
+    ctx = pg.Context(NX, NY, float(NX), float(NY), n, device=dev)
+    stream = ctx.stream()
+
+    # random-order upload, then a timed full sort
+    ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+    ctx.profile(True)
+    _, perm, _ = ctx.sort(perm=True)
+    ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+    ctx.sort()
+    sort_ms, sort_cnt = ctx.profile_read("sort")
+    sort_ms /= max(sort_cnt, 1)
+    # unsorted (random order) deposits for reference numbers: use the random-order upload
+    extras = {}
+    ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+    ctx.set_order(pg.ORDER_UNSORTED)
+    for nm in ("CIC", "TSC"):
+        for _ in range(2):
+            ctx.deposit(SCHEMES[nm], ESK_DT, download=False)
+        ctx.profile_read("deposit")
+        for _ in range(5):
+            ctx.deposit(SCHEMES[nm], ESK_DT, download=False)
+        ms, cnt = ctx.profile_read("deposit")
+        extras[f"{nm}_random_order"] = {"particles_per_s": n / (ms / cnt / 1e3), "kernel_ms": ms / cnt}
+    ctx.set_order(pg.ORDER_AUTO)
+    ctx.sort()
+    assert ctx.is_sorted()
+
+    # per-scheme sorted kernels
+    for nm, s in SCHEMES.items():
+        for _ in range(3):
+            ctx.deposit(s, ESK_DT, download=False)
+        ctx.profile_read("deposit")
+        for _ in range(20):
+            ctx.deposit(s, ESK_DT, download=False)
+        ms, cnt = ctx.profile_read("deposit")
+        bpp = BYTES_PER_PARTICLE_ESK if s == 3 else BYTES_PER_PARTICLE
+        kms = ms / cnt
+        extras[f"{nm}_sorted"] = {"particles_per_s": n / (kms / 1e3), "kernel_ms": kms,
+                                  "kernel_gbs": (bpp * n + BYTES_PER_CELL * G) / (kms / 1e3) / 1e9}
+    extras["sort_random_to_cells"] = {"ms": sort_ms, "particles_per_s": n / (sort_ms / 1e3),
+                                      "algorithmic_gbs": (48 * n + 4 * (G + 1)) / (sort_ms / 1e3) / 1e9}
+
+    # ---- timed region: K deposits of the sorted particles ----
+    for _ in range(args.warmup):
+        ctx.deposit(scheme, ESK_DT, download=False)
+    ctx.synchronize()
+    ctx.profile_read("deposit")
+    e0, e1 = ev.event(), ev.event()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.2)
+    launches0 = ctx.launch_count()
+    d.barrier()
+    ctx.synchronize()
+    ev.record(e0, stream)
+    for _ in range(args.steps):
+        ctx.deposit(scheme, ESK_DT, download=False)
+    ev.record(e1, stream)
+    ms = ev.elapsed_ms(e0, e1)
+    ctx.synchronize()
+    d.barrier()
+    launches = ctx.launch_count() - launches0
+    clk = clocks.stop()
+    kms_tot, kcnt = ctx.profile_read("deposit")
+    ms_max = d.max(ms)
+    value = n * args.steps * d.ws / (ms_max / 1e3)
+    kernel_ms = kms_tot / max(kcnt, 1)
+    alg_bytes = BYTES_PER_PARTICLE * n + BYTES_PER_CELL * G
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
+    traffic = traffic_from_profile()
+
+    # ---- e2e: host buffers through the C ABI (upload x,y,q + deposit + rho download) ----
+    order = perm.astype(np.int64)
+    pin = {k: pg.PinnedArray(n) for k in ("x", "y", "q")}
+    for k in pin:
+        pin[k].array[:] = p[k][order]
+    rho_host = pg.PinnedArray(G)
+    e2e_steps = max(3, min(args.steps, 20))
+    for _ in range(2):
+        ctx.upload(pin["x"].array, pin["y"].array, pin["q"].array)
+        pg._check(pg.lib().pic_gpu_deposit(ctx.h, scheme, ESK_DT, 0.0, pg._ptr(rho_host.array)))
+    assert ctx.is_sorted()
+    d.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.upload(pin["x"].array, pin["y"].array, pin["q"].array)
+        pg._check(pg.lib().pic_gpu_deposit(ctx.h, scheme, ESK_DT, 0.0, pg._ptr(rho_host.array)))
+    t_e2e = time.perf_counter() - t0
+    t_e2e = d.max(t_e2e)
+    e2e_value = n * e2e_steps * d.ws / t_e2e
+
+    # ---- CPU baseline (rank 0): the reference FP64 path on the host cores ----
+    cpu = None
+    if d.rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        run, kind = cpu_deposit_timer(threads)
+        ps = {k: v[order] for k, v in p.items()}
+        run(ps)
+        t_cpu, reps = 0.0, 0
+        while t_cpu < args.cpu_seconds or reps == 0:
+            t_cpu += run(ps)
+            reps += 1
+        cpu = {"value": n * reps / t_cpu, "unit": "particles/s", "cores": threads, "kind": kind,
+               "sample": f"full workload ({n} cell-sorted particles), FP64 CIC deposit x{reps}, "
+                         f"privatised OpenMP form of src/deposition/deposition_parallel.cpp"}
+    for a in list(pin.values()) + [rho_host]:
+        a.free()
+    ctx.close()
+    if d.rank != 0:
+        return None
+    return {
+        "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": d.ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64 fixed point (FP32 weights, FP64 rho)", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "grid": [NX, NY], "particles_per_cell": PPC, "particles": n,
+                   "density": "1+0.01cos(2*pi*x/1024)", "vth": VTH, "scheme": args.scheme,
+                   "l2": "inputs (1.07 GB particle stream) larger than L2; no flush", "parallelism": f"replicas{d.ws}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": traffic, "kernel": "deposit_tiled<CIC>",
+                     "kernel_ms": kernel_ms, "algorithmic_bytes_per_launch": alg_bytes},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "particles/s", "h2d_bytes_per_step": 24 * n,
+                "d2h_bytes_per_step": 8 * G, "steps": e2e_steps},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "extra": extras,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scheme", default="CIC", choices=list(SCHEMES))
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    d = Dist()
+    try:
+        res = run_reference(args, d) if args.impl == "reference" else run_gpu(args, d)
+    finally:
+        d.close()
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,153 @@
+/*
+ * pic_gb300.h -- C ABI of the GB300-native 2D electrostatic PIC deposition path.
+ *
+ * This ABI is the drop-in boundary for the hot path of ehocine/pic-deposition.
+ * Each entry point names the reference interface it replaces (file:line in that
+ * project). The reference's own GPU entry points are
+ *   void pic::depositChargeCudaSoA(const ParticlesSoA&, FieldGrid&, const DepositionConfig&)
+ *   (src/deposition/cuda/deposition_cuda.hpp:11-12, deposition_cuda.cu:288-337),
+ * which copy host arrays to the device on every call; here particle and grid
+ * state stays resident in a context between calls and host copies happen only
+ * in the upload/download calls and in calls given a non-NULL host pointer.
+ *
+ * Conventions
+ *  - Every function returns an int status: PIC_OK (0) or a negative PIC_ERR_*.
+ *    No C++ exception crosses the ABI. pic_gpu_last_error() gives the message of
+ *    the calling thread's last failure.
+ *  - A context is bound to one CUDA device and one stream; it is not thread-safe
+ *    (the caller serialises calls), like the reference's single-threaded API.
+ *  - Host pointers are plain arrays; lengths are element counts. Device state is
+ *    opaque.
+ *  - Particles are stored on the device as FP32 offsets inside their cell plus a
+ *    u32 cell key iy*Nx+ix; the key is computed from the FP64 host position with
+ *    the reference's Domain::cellCoords (src/pic/domain.hpp:34-43), so keys are
+ *    bit-identical to pic::particleCellIndex (src/sorting/cell_sort.cpp:8-13).
+ *  - Charge is deposited in fixed point: each stencil contribution
+ *    q*w*2^24/max|q| is rounded to the nearest integer and summed in int64, so
+ *    rho is independent of summation order and bit-identical run to run. One
+ *    unit of the int64 grid is inv_vol/cq, cq = (float)2^24 / max|q|
+ *    (returned by pic_gpu_get_rho_fixed).
+ */
+#ifndef PIC_GB300_H
+#define PIC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define PIC_OK 0
+#define PIC_ERR_ARG (-1)         /* bad argument (NULL, size, scheme, ...)              */
+#define PIC_ERR_CUDA (-2)        /* a CUDA runtime / cuFFT call failed                  */
+#define PIC_ERR_NOMEM (-3)       /* device or pinned allocation failed                  */
+#define PIC_ERR_STATE (-4)       /* call out of order (e.g. deposit before upload)      */
+#define PIC_ERR_OVERFLOW (-5)    /* fixed-point headroom would be exceeded              */
+#define PIC_ERR_COURANT (-6)     /* Esirkepov current needs |v|*dt < cell size          */
+#define PIC_ERR_TIMEOUT (-7)     /* a bounded device-side wait gave up                  */
+#define PIC_ERR_UNSUPPORTED (-8) /* valid request this build does not support           */
+#define PIC_ERR_DEVICE (-9)      /* a kernel reported bad data (non-finite position ...) */
+
+/* ---- schemes: values of pic::DepositionScheme (src/deposition/deposition.hpp:11) ---- */
+#define PIC_SCHEME_NGP 0
+#define PIC_SCHEME_CIC 1
+#define PIC_SCHEME_TSC 2
+#define PIC_SCHEME_ESIRKEPOV 3 /* the reference's trajectory-averaged rho (ngp.cpp:13-84) */
+
+/* ---- deposit ordering modes ---- */
+#define PIC_ORDER_AUTO 0     /* tiled shared-memory kernel when cell-sorted, else atomic kernel */
+#define PIC_ORDER_SORTED 1   /* require cell-sorted particles (PIC_ERR_STATE otherwise)        */
+#define PIC_ORDER_UNSORTED 2 /* global-atomic kernel regardless of order                        */
+
+/* Mirrors pic::Domain (src/pic/domain.hpp:7-44): periodic box [0,Lx)x[0,Ly),
+ * Nx x Ny cells, dx = Lx/Nx, dy = Ly/Ny. */
+typedef struct pic_domain {
+    double Lx;
+    double Ly;
+    int32_t Nx;
+    int32_t Ny;
+} pic_domain;
+
+typedef struct pic_ctx pic_ctx;
+
+/* Mirrors pic::Diagnostics (src/pic/diagnostics.hpp:8-15), FP64 sums on the GPU. */
+typedef struct pic_diag {
+    double charge_error;
+    double total_charge;
+    double integrated_rho;
+    double kinetic_energy;
+    double field_energy;
+    double total_energy;
+} pic_diag;
+
+/* ---- context ---- */
+
+/* Creates a context on `device` for up to `capacity` particles. Replaces the
+ * reference's static never-freed device pool (deposition_cuda.cu:243-273). */
+int pic_gpu_create(const pic_domain* domain, size_t capacity, int device, pic_ctx** out);
+int pic_gpu_destroy(pic_ctx* ctx);
+const char* pic_gpu_last_error(void);
+int pic_gpu_synchronize(pic_ctx* ctx);
+/* Number of kernels this library launched on the context since creation. */
+int pic_gpu_launch_count(pic_ctx* ctx, long long* out);
+/* The context's CUDA stream (cudaStream_t), for callers that time on it. */
+int pic_gpu_get_stream(pic_ctx* ctx, void** stream_out);
+/* CUDA-event timing of the library's dominant kernels on the context stream.
+ * While enabled, every launch of a named kernel ("deposit", "sort", ...) is
+ * bracketed by two events; pic_gpu_profile_read synchronises, returns the summed
+ * milliseconds and launch count for `kernel` and forgets those records. The
+ * reference times whole calls with std::chrono (deposition.cpp:257-310). */
+int pic_gpu_profile_enable(pic_ctx* ctx, int enable);
+int pic_gpu_profile_read(pic_ctx* ctx, const char* kernel, double* total_ms, long long* launches);
+
+/* Page-locked host buffers for fast uploads/downloads (cudaHostAlloc / cudaFreeHost). */
+int pic_gpu_host_alloc(size_t bytes, void** out);
+int pic_gpu_host_free(void* p);
+
+/* ---- particles ---- */
+
+/* Uploads FP64 SoA particles (layout of pic::ParticlesSoA, src/pic/particles.hpp:45-83)
+ * and converts them to the device layout. vx, vy, m may be NULL (0, 0, 1).
+ * Replaces the per-call H2D copies of deposition_cuda.cu:296-303. Marks the
+ * particles unsorted. */
+int pic_gpu_upload_particles(pic_ctx* ctx, const double* x, const double* y, const double* vx, const double* vy,
+                             const double* q, const double* m, size_t n);
+/* Downloads particles back to FP64 SoA (positions rebuilt as (ix+xr)*dx). Any pointer may be NULL. */
+int pic_gpu_download_particles(pic_ctx* ctx, double* x, double* y, double* vx, double* vy, double* q, double* m);
+/* Raw device layout, for bit-exact parity checks: any pointer may be NULL. */
+int pic_gpu_download_device_layout(pic_ctx* ctx, uint32_t* cell, float* xr, float* yr, float* vx, float* vy,
+                                   float* q);
+int pic_gpu_num_particles(pic_ctx* ctx, size_t* n_out);
+/* 1 when the resident particles are in cell order with valid per-cell offsets
+ * (after pic_gpu_sort, or after an upload whose keys were already non-decreasing). */
+int pic_gpu_is_sorted(pic_ctx* ctx, int* sorted_out);
+
+/* ---- cell sort: replaces pic::sortParticlesByCell(ParticlesSoA&, const Domain&)
+ *      (src/sorting/cell_sort.hpp:8-11, cell_sort.cpp:22-46) ---- */
+
+/* Stable LSD radix sort of the resident particles by cell key, in place.
+ * Optional host outputs: sorted keys (n), permutation (n; perm[i] = pre-sort
+ * index of the particle now at i) and per-cell offsets (Nx*Ny+1). */
+int pic_gpu_sort(pic_ctx* ctx, uint32_t* keys_out, uint32_t* perm_out, uint32_t* offsets_out);
+
+/* ---- deposition: replaces pic::depositChargeSoA / depositKernelSoA's backend
+ *      dispatch (src/deposition/deposition.cpp:120-132,181-200) ---- */
+
+int pic_gpu_set_deposit_order(pic_ctx* ctx, int order);
+/* Tile of the sorted kernel, in cells (tile_w <= 64, tile_h <= 32). */
+int pic_gpu_set_tile(pic_ctx* ctx, int tile_w, int tile_h);
+/* Deposits rho for `scheme` (PIC_SCHEME_*) into the context's grid, adds
+ * `background` to every node, and copies rho to `rho_out` (Nx*Ny doubles)
+ * when non-NULL. `dt` is DepositionConfig::esirkepov_dt (deposition.hpp:23). */
+int pic_gpu_deposit(pic_ctx* ctx, int scheme, double dt, double background, double* rho_out);
+/* The int64 fixed-point grid of the last deposit and its unit (rho = acc*unit + background). */
+int pic_gpu_get_rho_fixed(pic_ctx* ctx, int64_t* acc_out, double* unit_out);
+int pic_gpu_get_rho(pic_ctx* ctx, double* rho_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,389 @@
+"""CPU oracle for the GB300 PIC deposition path -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
+legs may import this module, and only as the checker or the timed CPU
+baseline; the product never does.
+
+Two backends:
+  * ``Port``  -- ctypes over ``oracle/liboracle.so``, this project's C
+    restatement of the reference algorithms (pic_oracle.c, each function
+    citing the reference file:line) plus the exact restatement of the GPU
+    fixed-point arithmetic. Builds anywhere (``make -C oracle port``).
+  * ``Ref``   -- ctypes over ``oracle/_ref/libpicref.so``, the reference's own
+    sources compiled by ``make -C oracle ref`` (only where the reference
+    checkout exists).
+
+FFT-based pieces are restated in numpy:
+  * ``spectral_noise``   -- diagnostics.cpp:53-102 (FFTW R2HC x R2HC power ratio)
+  * ``poisson_fft``      -- poisson_fft.cpp:23-35,45-94 (continuous k^2, DC=0)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libpicref.so")
+REFERENCE_SRC = "/root/reference"
+
+NGP, CIC, TSC, ESIRKEPOV = 0, 1, 2, 3
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+
+
+class _Domain(C.Structure):
+    _fields_ = [("Lx", C.c_double), ("Ly", C.c_double), ("Nx", C.c_int32), ("Ny", C.c_int32)]
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile the port (always) and the reference library (when the reference checkout is present)."""
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    if ref is None:
+        ref = os.path.isdir(REFERENCE_SRC)
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_SRC}"], check=True)
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+class Port:
+    """The project's C restatement (liboracle.so)."""
+
+    def __init__(self, path: str = PORT_LIB):
+        if not os.path.exists(path):
+            build(ref=False)
+        L = C.CDLL(path)
+        self.lib = L
+        D = C.POINTER(_Domain)
+        L.orc_init_particles.argtypes = [C.c_int, D, C.c_size_t, C.c_double, C.c_double, C.c_int, C.c_uint32,
+                                         _dp, _dp, _dp, _dp, _dp, _dp]
+        L.orc_particle_cell_index.argtypes = [D, C.c_double, C.c_double]
+        L.orc_deposit_ref.argtypes = [D, C.c_int, C.c_size_t, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, _dp]
+        L.orc_stable_cell_sort.argtypes = [D, C.c_size_t, _dp, _dp, _u32p, _u32p, _u32p]
+        L.orc_stable_sort_keys.argtypes = [C.c_size_t, C.c_uint32, _u32p, _u32p, _u32p, _u32p]
+        L.orc_gather_ref.argtypes = [D, C.c_size_t, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double]
+        L.orc_push_ref.argtypes = [D, C.c_size_t, _dp, _dp, _dp, _dp, C.c_double]
+        L.orc_gs_ref.argtypes = [D, _dp, C.c_int, C.c_double, _dp, _dp, _dp]
+        L.orc_efield.argtypes = [D, _dp, _dp, _dp]
+        L.orc_rbgs.argtypes = [D, _dp, _dp, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int),
+                               C.POINTER(C.c_double)]
+        L.orc_rbgs_residual.argtypes = [D, _dp, _dp]
+        L.orc_rbgs_residual.restype = C.c_double
+        for f in ("orc_integrated_rho",):
+            getattr(L, f).argtypes = [D, _dp]
+            getattr(L, f).restype = C.c_double
+        L.orc_field_energy.argtypes = [D, _dp, _dp]
+        L.orc_field_energy.restype = C.c_double
+        L.orc_to_device.argtypes = [D, C.c_size_t, _dp, _dp, _u32p, _fp, _fp]
+        L.orc_fixed_charge_factor.argtypes = [C.c_size_t, _fp]
+        L.orc_fixed_charge_factor.restype = C.c_float
+        L.orc_deposit_fixed.argtypes = [D, C.c_int, C.c_size_t, _u32p, _fp, _fp, _fp, _fp, _fp, C.c_double, _i64p,
+                                        C.POINTER(C.c_double)]
+        L.orc_fixed_to_rho.argtypes = [C.c_size_t, _i64p, C.c_double, C.c_double, _dp]
+
+    @staticmethod
+    def dom(nx, ny, lx, ly):
+        return C.byref(_Domain(float(lx), float(ly), int(nx), int(ny)))
+
+    # ---- reference restatements ----
+    def init_particles(self, kind, nx, ny, lx, ly, n, p0=1.0, p1=0.0, mode=1, seed=42):
+        out = [np.zeros(n) for _ in range(6)]
+        rc = self.lib.orc_init_particles(kind, self.dom(nx, ny, lx, ly), n, p0, p1, mode, seed, *out)
+        assert rc == 0
+        return dict(zip(("x", "y", "vx", "vy", "q", "m"), out))
+
+    def cell_index(self, nx, ny, lx, ly, x, y):
+        return self.lib.orc_particle_cell_index(self.dom(nx, ny, lx, ly), x, y)
+
+    def deposit_ref(self, nx, ny, lx, ly, scheme, p, dt=0.0, threads=1):
+        rho = np.zeros(nx * ny)
+        n = len(p["x"])
+        vx = p.get("vx", np.zeros(n))
+        vy = p.get("vy", np.zeros(n))
+        rc = self.lib.orc_deposit_ref(self.dom(nx, ny, lx, ly), scheme, n, _c(p["x"], np.float64),
+                                      _c(p["y"], np.float64), _c(vx, np.float64), _c(vy, np.float64),
+                                      _c(p["q"], np.float64), dt, threads, rho)
+        assert rc == 0
+        return rho
+
+    def stable_cell_sort(self, nx, ny, lx, ly, x, y):
+        n = len(x)
+        keys = np.zeros(n, np.uint32)
+        perm = np.zeros(n, np.uint32)
+        offs = np.zeros(nx * ny + 1, np.uint32)
+        rc = self.lib.orc_stable_cell_sort(self.dom(nx, ny, lx, ly), n, _c(x, np.float64), _c(y, np.float64), keys,
+                                           perm, offs)
+        assert rc == 0
+        return keys, perm, offs
+
+    def stable_sort_keys(self, keys, nkeys):
+        keys = _c(keys, np.uint32)
+        n = len(keys)
+        ks = np.zeros(n, np.uint32)
+        perm = np.zeros(n, np.uint32)
+        offs = np.zeros(nkeys + 1, np.uint32)
+        rc = self.lib.orc_stable_sort_keys(n, nkeys, keys, ks, perm, offs)
+        assert rc == 0
+        return ks, perm, offs
+
+    def gather_ref(self, nx, ny, lx, ly, p, ex, ey, dt):
+        vx = _c(p["vx"], np.float64).copy()
+        vy = _c(p["vy"], np.float64).copy()
+        n = len(vx)
+        m = p.get("m", np.ones(n))
+        self.lib.orc_gather_ref(self.dom(nx, ny, lx, ly), n, _c(p["x"], np.float64), _c(p["y"], np.float64), vx, vy,
+                                _c(p["q"], np.float64), _c(m, np.float64), _c(ex, np.float64), _c(ey, np.float64), dt)
+        return vx, vy
+
+    def push_ref(self, nx, ny, lx, ly, p, dt):
+        x = _c(p["x"], np.float64).copy()
+        y = _c(p["y"], np.float64).copy()
+        self.lib.orc_push_ref(self.dom(nx, ny, lx, ly), len(x), x, y, _c(p["vx"], np.float64),
+                              _c(p["vy"], np.float64), dt)
+        return x, y
+
+    def gs_ref(self, nx, ny, lx, ly, rho, max_iters=500, tol=1e-6):
+        phi, ex, ey = np.zeros(nx * ny), np.zeros(nx * ny), np.zeros(nx * ny)
+        it = self.lib.orc_gs_ref(self.dom(nx, ny, lx, ly), _c(rho, np.float64), max_iters, tol, phi, ex, ey)
+        return phi, ex, ey, it
+
+    def efield(self, nx, ny, lx, ly, phi):
+        ex, ey = np.zeros(nx * ny), np.zeros(nx * ny)
+        self.lib.orc_efield(self.dom(nx, ny, lx, ly), _c(phi, np.float64), ex, ey)
+        return ex, ey
+
+    def rbgs(self, nx, ny, lx, ly, rho, phi0=None, tol=1e-8, max_iters=100000, check_every=1):
+        phi = np.zeros(nx * ny) if phi0 is None else _c(phi0, np.float64).copy()
+        it = C.c_int(0)
+        res = C.c_double(0)
+        rc = self.lib.orc_rbgs(self.dom(nx, ny, lx, ly), _c(rho, np.float64), phi, tol, max_iters, check_every,
+                               C.byref(it), C.byref(res))
+        assert rc == 0
+        return phi, it.value, res.value
+
+    def rbgs_residual(self, nx, ny, lx, ly, b, phi):
+        return self.lib.orc_rbgs_residual(self.dom(nx, ny, lx, ly), _c(b, np.float64), _c(phi, np.float64))
+
+    def integrated_rho(self, nx, ny, lx, ly, rho):
+        return self.lib.orc_integrated_rho(self.dom(nx, ny, lx, ly), _c(rho, np.float64))
+
+    def field_energy(self, nx, ny, lx, ly, ex, ey):
+        return self.lib.orc_field_energy(self.dom(nx, ny, lx, ly), _c(ex, np.float64), _c(ey, np.float64))
+
+    # ---- GPU-arithmetic restatements ----
+    def to_device(self, nx, ny, lx, ly, x, y):
+        n = len(x)
+        cell = np.zeros(n, np.uint32)
+        xr = np.zeros(n, np.float32)
+        yr = np.zeros(n, np.float32)
+        self.lib.orc_to_device(self.dom(nx, ny, lx, ly), n, _c(x, np.float64), _c(y, np.float64), cell, xr, yr)
+        return cell, xr, yr
+
+    def fixed_charge_factor(self, q32):
+        q32 = _c(q32, np.float32)
+        return self.lib.orc_fixed_charge_factor(len(q32), q32)
+
+    def deposit_fixed(self, nx, ny, lx, ly, scheme, cell, xr, yr, q32, vx32=None, vy32=None, dt=0.0):
+        n = len(cell)
+        if vx32 is None:
+            vx32 = np.zeros(n, np.float32)
+        if vy32 is None:
+            vy32 = np.zeros(n, np.float32)
+        acc = np.zeros(nx * ny, np.int64)
+        unit = C.c_double(0)
+        rc = self.lib.orc_deposit_fixed(self.dom(nx, ny, lx, ly), scheme, n, _c(cell, np.uint32), _c(xr, np.float32),
+                                        _c(yr, np.float32), _c(vx32, np.float32), _c(vy32, np.float32),
+                                        _c(q32, np.float32), dt, acc, C.byref(unit))
+        assert rc == 0
+        return acc, unit.value
+
+    @staticmethod
+    def fixed_to_rho(acc, unit, background=0.0):
+        return acc.astype(np.float64) * unit + background
+
+
+class Ref:
+    """The reference's own sources (oracle/_ref/libpicref.so)."""
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(REF_LIB)
+
+    def __init__(self, path: str = REF_LIB):
+        L = C.CDLL(path)
+        self.lib = L
+        L.ref_init_particles.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_size_t, C.c_double,
+                                         C.c_double, C.c_int, C.c_uint, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.ref_cell_index.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]
+        L.ref_deposit.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double,
+                                  C.c_size_t, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.ref_deposit_timed.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                        C.c_double, C.c_int, C.c_size_t, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.ref_sort.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_size_t, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.ref_gather.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_size_t, _dp, _dp, _dp, _dp, _dp, _dp,
+                                 _dp, _dp, C.c_double]
+        L.ref_push.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_size_t, _dp, _dp, _dp, _dp, C.c_double]
+        L.ref_poisson_gs.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp, C.c_int, C.c_double, _dp, _dp,
+                                     _dp]
+        L.ref_poisson_fft.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, _dp]
+        L.ref_spectral_noise.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
+        L.ref_spectral_noise.restype = C.c_double
+        L.ref_simulation_run.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                         C.c_int, C.c_size_t, C.c_uint, C.c_int, C.c_double, C.c_double, C.c_int,
+                                         C.c_double, C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _dp,
+                                         C.POINTER(C.c_double)]
+        L.ref_langmuir_validation.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                              C.c_size_t, C.c_double, C.c_int, _dp]
+
+    def init_particles(self, kind, nx, ny, lx, ly, n, p0=1.0, p1=0.0, mode=1, seed=42):
+        out = [np.zeros(n) for _ in range(6)]
+        rc = self.lib.ref_init_particles(kind, nx, ny, lx, ly, n, p0, p1, mode, seed, *out)
+        assert rc == 0
+        return dict(zip(("x", "y", "vx", "vy", "q", "m"), out))
+
+    def deposit(self, nx, ny, lx, ly, scheme, p, dt=0.0, sorted_=False, threads=1):
+        rho = np.zeros(nx * ny)
+        n = len(p["x"])
+        vx = p.get("vx", np.zeros(n))
+        vy = p.get("vy", np.zeros(n))
+        m = p.get("m", np.ones(n))
+        rc = self.lib.ref_deposit(nx, ny, lx, ly, scheme, int(sorted_), threads, dt, n, _c(p["x"], np.float64),
+                                  _c(p["y"], np.float64), _c(vx, np.float64), _c(vy, np.float64),
+                                  _c(p["q"], np.float64), _c(m, np.float64), rho)
+        assert rc == 0
+        return rho
+
+    def deposit_timed(self, nx, ny, lx, ly, scheme, p, dt=0.0, sorted_=False, threads=1, repeats=5):
+        st = np.zeros(6)
+        n = len(p["x"])
+        rc = self.lib.ref_deposit_timed(nx, ny, lx, ly, scheme, int(sorted_), threads, dt, repeats, n,
+                                        _c(p["x"], np.float64), _c(p["y"], np.float64), _c(p["vx"], np.float64),
+                                        _c(p["vy"], np.float64), _c(p["q"], np.float64), _c(p["m"], np.float64), st)
+        assert rc == 0
+        return dict(zip(("sort_ms", "deposit_ms", "deposit_std_ms", "throughput", "bandwidth_gbs", "charge_error"),
+                        st.tolist()))
+
+    def sort(self, nx, ny, lx, ly, p):
+        arrs = [_c(p[k], np.float64).copy() for k in ("x", "y", "vx", "vy", "q", "m")]
+        rc = self.lib.ref_sort(nx, ny, lx, ly, len(arrs[0]), *arrs)
+        assert rc == 0
+        return dict(zip(("x", "y", "vx", "vy", "q", "m"), arrs))
+
+    def gather(self, nx, ny, lx, ly, p, ex, ey, dt):
+        vx = _c(p["vx"], np.float64).copy()
+        vy = _c(p["vy"], np.float64).copy()
+        self.lib.ref_gather(nx, ny, lx, ly, len(vx), _c(p["x"], np.float64), _c(p["y"], np.float64), vx, vy,
+                            _c(p["q"], np.float64), _c(p["m"], np.float64), _c(ex, np.float64),
+                            _c(ey, np.float64), dt)
+        return vx, vy
+
+    def push(self, nx, ny, lx, ly, p, dt):
+        x = _c(p["x"], np.float64).copy()
+        y = _c(p["y"], np.float64).copy()
+        self.lib.ref_push(nx, ny, lx, ly, len(x), x, y, _c(p["vx"], np.float64), _c(p["vy"], np.float64), dt)
+        return x, y
+
+    def poisson_gs(self, nx, ny, lx, ly, rho, max_iters=500, tol=1e-6):
+        out = [np.zeros(nx * ny) for _ in range(3)]
+        self.lib.ref_poisson_gs(nx, ny, lx, ly, _c(rho, np.float64), max_iters, tol, *out)
+        return tuple(out)
+
+    def poisson_fft(self, nx, ny, lx, ly, rho):
+        out = [np.zeros(nx * ny) for _ in range(3)]
+        self.lib.ref_poisson_fft(nx, ny, lx, ly, _c(rho, np.float64), *out)
+        return tuple(out)
+
+    def spectral_noise(self, nx, ny, lx, ly, rho):
+        return self.lib.ref_spectral_noise(nx, ny, lx, ly, _c(rho, np.float64))
+
+    def simulation_run(self, nx, ny, lx, ly, dt, steps, scheme, n, seed=42, mode=0, temperature=1.0,
+                       amplitude=0.01, mode_number=1, landau_temperature=0.1, beam_velocity=0.3,
+                       perturbation=0.01, sorted_=False, poisson_gs=False):
+        te, ke, fe, ce = (np.zeros(steps) for _ in range(4))
+        drift = C.c_double(0)
+        rc = self.lib.ref_simulation_run(nx, ny, lx, ly, dt, steps, scheme, int(poisson_gs), n, seed, mode,
+                                         temperature, amplitude, mode_number, landau_temperature, beam_velocity,
+                                         perturbation, int(sorted_), te, ke, fe, ce, C.byref(drift))
+        assert rc == 0
+        return dict(total=te, kinetic=ke, field=fe, charge_error=ce, drift=drift.value)
+
+    def langmuir_validation(self, nx, ny, lx, ly, dt, steps, scheme, n, amplitude=0.01, mode_number=1):
+        out = np.zeros(5)
+        rc = self.lib.ref_langmuir_validation(nx, ny, lx, ly, dt, steps, scheme, n, amplitude, mode_number, out)
+        assert rc == 0
+        return dict(zip(("omega_theory", "omega_measured", "relative_error", "omega_ratio", "amplitude_decay"),
+                        out.tolist()))
+
+
+# ---------------------------------------------------------------------------
+# numpy restatements of the FFT-based reference pieces
+# ---------------------------------------------------------------------------
+def _r2hc_1d(a: np.ndarray, axis: int) -> np.ndarray:
+    """FFTW R2HC along ``axis``: Re X_k at k <= n/2, Im X_k at n-k for 0 < k < (n+1)/2."""
+    n = a.shape[axis]
+    X = np.fft.fft(a, axis=axis)
+    out = np.empty_like(a, dtype=np.float64)
+    idx = [slice(None)] * a.ndim
+
+    def put(k_dst, vals):
+        idx[axis] = k_dst
+        out[tuple(idx)] = vals
+
+    def take(k):
+        idx[axis] = k
+        return X[tuple(idx)]
+
+    for k in range(0, n // 2 + 1):
+        put(k, take(k).real)
+    for k in range(1, (n + 1) // 2):
+        put(n - k, take(k).imag)
+    return out
+
+
+def spectral_noise(nx: int, ny: int, rho: np.ndarray) -> float:
+    """spectralNoiseLevel, src/pic/diagnostics.cpp:53-102: high-k fraction of the
+    R2HC x R2HC power of rho, cut at kx >= nx/3 or ky >= ny/3."""
+    a = np.asarray(rho, np.float64).reshape(ny, nx)
+    out = _r2hc_1d(_r2hc_1d(a, 1), 0)
+    power = out * out
+    kcx = max(1, nx // 3)
+    kcy = max(1, ny // 3)
+    i = np.arange(nx)
+    j = np.arange(ny)
+    kx = np.where(i <= nx // 2, i, nx - i)
+    ky = np.where(j <= ny // 2, j, ny - j)
+    high = (kx[None, :] >= kcx) | (ky[:, None] >= kcy)
+    total = power.sum()
+    if total <= 1e-30:
+        return 0.0
+    return float(power[high].sum() / total)
+
+
+def poisson_fft(nx: int, ny: int, lx: float, ly: float, rho: np.ndarray):
+    """PoissonSolverFFT::solve, src/pic/poisson_fft.cpp:45-94: phi_hat =
+    (rho*dV)_hat / k^2 with continuous k = 2*pi*m/L, DC set to 0, then the
+    forward-difference E. Returns (phi, Ex, Ey) flattened."""
+    dx, dy = lx / nx, ly / ny
+    a = np.asarray(rho, np.float64).reshape(ny, nx) * (dx * dy)
+    F = np.fft.fft2(a)
+    i = np.arange(nx)
+    j = np.arange(ny)
+    kx = 2.0 * np.pi * np.where(i <= nx // 2, i, i - nx) / lx
+    ky = 2.0 * np.pi * np.where(j <= ny // 2, j, j - ny) / ly
+    k2 = kx[None, :] ** 2 + ky[:, None] ** 2
+    k2[0, 0] = 1.0
+    F = F / k2
+    F[0, 0] = 0.0
+    phi = np.fft.ifft2(F).real
+    ex = -(np.roll(phi, -1, axis=1) - phi) / dx
+    ey = -(np.roll(phi, -1, axis=0) - phi) / dy
+    return phi.ravel(), ex.ravel(), ey.ravel()

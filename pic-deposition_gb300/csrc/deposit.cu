@@ -1,0 +1,544 @@
+// Charge deposition: NGP / CIC / TSC / trajectory-averaged ("Esirkepov") rho.
+//
+// Replaces the reference's CPU kernels (src/deposition/ngp.cpp:108-228) and its
+// CUDA backend (src/deposition/cuda/deposition_cuda.cu:205-241: one thread per
+// particle with FP64 global atomics, or one block per tile scanning all
+// particles). Design:
+//
+//  * Fixed point. Each stencil value (q*cq*Y[j])*X[i] (FP32, cq = 2^24/max|q|)
+//    is rounded to the nearest int32 and summed in int64, so the result does
+//    not depend on summation order: the tiled, atomic and oracle paths agree
+//    bit for bit. |value| <= 2^24, so a warp-wide partial sum fits in int32.
+//  * Sorted path (deposit_tiled). One CTA per tile of tile_w x tile_h cells;
+//    its int64 accumulators (tile + halo of 1 cell below, 2 above) live in
+//    shared memory. Warp w walks rows w, w+8, ... of the tile; the particles of
+//    one row of the tile are one contiguous run of the cell-sorted stream,
+//    [offsets[c0], offsets[c0+tile_w]). Each warp step loads 32 particles
+//    coalesced (streaming loads, the particle stream is read once), computes
+//    every lane's stencil frame, and combines lanes of the same cell before any
+//    atomic: with one or two cells in the step, a transposed warp reduction
+//    leaves each frame node's warp total in one lane (V values in about V
+//    shuffles), and those lanes issue one shared atomic each. Steps with three
+//    or more cells fall back to per-lane shared atomics. At the end the tile
+//    is flushed to the global int64 grid with one atomic per non-zero node.
+//  * Unsorted path (deposit_atomic): one thread per particle, int64 atomics
+//    straight into the L2-resident global grid.
+//
+// Stencil frames (weights relative to the particle's own cell, identical to the
+// oracle's restatement):
+//   NGP   2 nodes (0..1)  one-hot at offset (r >= 0.5)             ngp.cpp:108-120
+//   CIC   2 nodes (0..1)  (1-r, r)                                 ngp.cpp:140-157
+//   TSC   4 nodes (-1..2) tscWeights written in cell-relative form ngp.cpp:28-34,181-202
+//   ESK   3 nodes (-1..1) path r -> r + v*dt/dx split at cell     ngp.cpp:36-84,216-228
+//         boundaries, weights = piece / path; static (|v*dt| < 1e-15) -> CIC.
+//         Moves of a cell or more go through a general per-lane loop with
+//         global atomics.
+//
+// Compiled with --fmad=false: no multiply-add is fused, so every FP32 result
+// equals the oracle's (compiled with -ffp-contract=off).
+#include "pic_internal.cuh"
+
+namespace picgb {
+
+enum { S_NGP = 0, S_CIC = 1, S_TSC = 2, S_ESK = 3 };
+
+template <int S>
+struct Frame;
+template <>
+struct Frame<S_NGP> {
+    static constexpr int NX = 2, LO = 0, V = 4;
+};
+template <>
+struct Frame<S_CIC> {
+    static constexpr int NX = 2, LO = 0, V = 4;
+};
+template <>
+struct Frame<S_TSC> {
+    static constexpr int NX = 4, LO = -1, V = 16;
+};
+template <>
+struct Frame<S_ESK> {
+    static constexpr int NX = 3, LO = -1, V = 16;
+};
+
+constexpr int DEP_THREADS = 256;
+constexpr int DEP_WARPS = DEP_THREADS / 32;
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int ESK_GEN_CAP = 256;
+
+struct DepArgs {
+    const uint32_t* cell;
+    const float* xr;
+    const float* yr;
+    const float* vx;
+    const float* vy;
+    const float* q;
+    const uint32_t* offsets;
+    unsigned long long* acc;
+    size_t n;
+    int Nx, Ny;
+    float dtf, dtdx, dtdy;
+    int tile_w, tile_h, tiles_x;
+    DevStats* st;
+};
+
+// ---- one axis of a frame. Returns false when an Esirkepov move needs the general loop.
+template <int S>
+__device__ __forceinline__ bool axis_frame(float r, float v, float dtf, float dtd, float (&X)[Frame<S>::NX]) {
+    if constexpr (S == S_NGP) {
+        X[0] = r >= 0.5f ? 0.0f : 1.0f;
+        X[1] = r >= 0.5f ? 1.0f : 0.0f;
+        return true;
+    } else if constexpr (S == S_CIC) {
+        X[0] = 1.0f - r;
+        X[1] = r;
+        return true;
+    } else if constexpr (S == S_TSC) {
+        if (r < 0.5f) {
+            const float d0 = 0.5f - r, d2 = 0.5f + r;
+            X[0] = 0.5f * (d0 * d0);
+            X[1] = 0.75f - r * r;
+            X[2] = 0.5f * (d2 * d2);
+            X[3] = 0.0f;
+        } else {
+            const float d0 = 1.5f - r, d1 = r - 1.0f, d2 = r - 0.5f;
+            X[0] = 0.0f;
+            X[1] = 0.5f * (d0 * d0);
+            X[2] = 0.75f - d1 * d1;
+            X[3] = 0.5f * (d2 * d2);
+        }
+        return true;
+    } else {
+        if (fabsf(v * dtf) < 1e-15f) {
+            X[0] = 0.0f;
+            X[1] = 1.0f - r;
+            X[2] = r;
+            return true;
+        }
+        const float dc = v * dtd;
+        if (!(fabsf(dc) < 1.0f)) return false;
+        const float e = r + dc;
+        X[0] = 0.0f;
+        X[1] = 1.0f;
+        X[2] = 0.0f;
+        if (dc > 0.0f) {
+            if (e > 1.0f) {
+                const float wb = __fdiv_rn(e - 1.0f, e - r);
+                X[1] = 1.0f - wb;
+                X[2] = wb;
+            }
+        } else if (e < 0.0f) {
+            const float wl = __fdiv_rn(0.0f - e, r - e);
+            X[0] = wl;
+            X[1] = 1.0f - wl;
+        }
+        return true;
+    }
+}
+
+// General trajectory split (moves of one cell or more), one piece per call.
+struct SegIter {
+    float r, e, tot, s;
+    int c, dir, k;
+    __device__ void init(float r0, float v, float dtf, float dtd) {
+        r = r0;
+        k = 0;
+        if (fabsf(v * dtf) < 1e-15f) {
+            dir = 0;
+            return;
+        }
+        const float dc = v * dtd;
+        e = r0 + dc;
+        dir = dc > 0.0f ? 1 : -1;
+        tot = dir > 0 ? e - r0 : r0 - e;
+        s = r0;
+        c = 0;
+    }
+    __device__ bool next(int& off, float& w) {
+        if (dir == 0) {
+            if (k == 0) {
+                off = 0;
+                w = 1.0f - r;
+                k = 1;
+                return true;
+            }
+            if (k == 1) {
+                off = 1;
+                w = r;
+                k = 2;
+                return true;
+            }
+            return false;
+        }
+        if (dir > 0) {
+            if (!(s < e)) return false;
+            const float b = (float)(c + 1);
+            const float nx = e < b ? e : b;
+            off = c;
+            w = __fdiv_rn(nx - s, tot);
+            s = nx;
+            ++c;
+        } else {
+            if (!(s > e)) return false;
+            const float b = (float)c;
+            const float nx = e > b ? e : b;
+            off = c;
+            w = __fdiv_rn(s - nx, tot);
+            s = nx;
+            --c;
+        }
+        ++k;
+        return true;
+    }
+};
+
+__device__ __noinline__ void esk_general_deposit(const DepArgs& a, int ix, int iy, float aq, float rx, float ry,
+                                                 float vxx, float vyy, size_t pidx) {
+    SegIter yi;
+    yi.init(ry, vyy, a.dtf, a.dtdy);
+    int oy, ox;
+    float wy, wx;
+    int ny = 0;
+    while (yi.next(oy, wy)) {
+        if (++ny > ESK_GEN_CAP) {
+            set_dev_error(a.st, DEV_MOVE_TOO_LARGE, (unsigned)pidx);
+            return;
+        }
+        const float ay = aq * wy;
+        const int gy = wrap_i(iy + oy, a.Ny);
+        SegIter xi;
+        xi.init(rx, vxx, a.dtf, a.dtdx);
+        int nx = 0;
+        while (xi.next(ox, wx)) {
+            if (++nx > ESK_GEN_CAP) {
+                set_dev_error(a.st, DEV_MOVE_TOO_LARGE, (unsigned)pidx);
+                return;
+            }
+            const int gx = wrap_i(ix + ox, a.Nx);
+            const long long v = __float2int_rn(ay * wx);
+            if (v) atomicAdd(a.acc + (size_t)gy * a.Nx + gx, (unsigned long long)v);
+        }
+    }
+}
+
+// Stencil values of one particle into val[0 .. NX*NX) (row-major j, i), zeros
+// elsewhere. Returns false if the particle took the general Esirkepov path
+// (already deposited, val all zero).
+template <int S>
+__device__ __forceinline__ bool particle_values(const DepArgs& a, size_t p, float cq, int ix, int iy,
+                                                int (&val)[Frame<S>::V]) {
+    constexpr int NX = Frame<S>::NX, V = Frame<S>::V;
+    const float rx = __ldcs(a.xr + p), ry = __ldcs(a.yr + p);
+    const float aq = __ldcs(a.q + p) * cq;
+    float vxx = 0.0f, vyy = 0.0f;
+    if constexpr (S == S_ESK) {
+        vxx = __ldcs(a.vx + p);
+        vyy = __ldcs(a.vy + p);
+    }
+    float X[NX], Y[NX];
+    const bool okx = axis_frame<S>(rx, vxx, a.dtf, a.dtdx, X);
+    const bool oky = axis_frame<S>(ry, vyy, a.dtf, a.dtdy, Y);
+#pragma unroll
+    for (int k = 0; k < V; ++k) val[k] = 0;
+    if (!(okx && oky)) {
+        esk_general_deposit(a, ix, iy, aq, rx, ry, vxx, vyy, p);
+        return false;
+    }
+#pragma unroll
+    for (int j = 0; j < NX; ++j) {
+        const float ay = aq * Y[j];
+#pragma unroll
+        for (int i = 0; i < NX; ++i) val[j * NX + i] = __float2int_rn(ay * X[i]);
+    }
+    return true;
+}
+
+// Transposed warp reduction of V int values per lane (V a power of two <= 32).
+// Afterwards every lane holds the warp total of value index lane >> (5 - log2 V)
+// in v[0]; the 32/V lanes that share an index hold the same total.
+template <int V>
+__device__ __forceinline__ int tr_reduce(int (&v)[V], int lane) {
+    constexpr int L = (V >= 32) ? 5 : (V >= 16) ? 4 : (V >= 8) ? 3 : (V >= 4) ? 2 : (V >= 2) ? 1 : 0;
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+        const int off = 16 >> s;
+        if (s < L) {
+            const int half = V >> (s + 1);
+            const bool upper = (lane & off) != 0;
+#pragma unroll
+            for (int i = 0; i < half; ++i) {
+                const int send = upper ? v[i] : v[i + half];
+                const int keep = upper ? v[i + half] : v[i];
+                v[i] = keep + __shfl_xor_sync(FULL, send, off);
+            }
+        } else {
+            v[0] += __shfl_xor_sync(FULL, v[0], off);
+        }
+    }
+    return v[0];
+}
+
+template <int V>
+struct Log2 {
+    static constexpr int value = (V >= 32) ? 5 : (V >= 16) ? 4 : (V >= 8) ? 3 : (V >= 4) ? 2 : (V >= 2) ? 1 : 0;
+};
+
+__device__ __forceinline__ void sadd(long long* s, int idx, int v) {
+    atomicAdd(reinterpret_cast<unsigned long long*>(s + idx), (unsigned long long)(long long)v);
+}
+
+template <int S>
+__global__ void __launch_bounds__(DEP_THREADS) deposit_tiled(DepArgs a) {
+    constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
+    constexpr int NV = NX * NX;
+    extern __shared__ long long sacc[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int SW = a.tile_w + 3;
+    const int tx = blockIdx.x % a.tiles_x, ty = blockIdx.x / a.tiles_x;
+    const int x0 = tx * a.tile_w, y0 = ty * a.tile_h;
+    const int tw = min(a.tile_w, a.Nx - x0), th = min(a.tile_h, a.Ny - y0);
+    const int nloc = (th + 3) * SW;
+    for (int i = threadIdx.x; i < nloc; i += DEP_THREADS) sacc[i] = 0;
+    __syncthreads();
+    const float cq = charge_factor(a.st);
+
+    for (int r = warp; r < th; r += DEP_WARPS) {
+        const int iy = y0 + r;
+        const uint32_t c0 = (uint32_t)iy * (uint32_t)a.Nx + (uint32_t)x0;
+        const uint32_t pbeg = a.offsets[c0], pend = a.offsets[c0 + tw];
+        const int lrow = r + 1 + LO;  // local row of frame row 0
+        for (uint32_t base = pbeg; base < pend; base += 32) {
+            const uint32_t p = base + lane;
+            const int nvalid = (int)min(pend - base, 32u);
+            int val[V];
+#pragma unroll
+            for (int k = 0; k < V; ++k) val[k] = 0;
+            uint32_t key = c0;
+            if (lane < nvalid) {
+                const uint32_t k = __ldcs(a.cell + p);
+                if (k - c0 < (uint32_t)tw) {
+                    key = k;
+                    particle_values<S>(a, p, cq, (int)(k - (uint32_t)iy * (uint32_t)a.Nx), iy, val);
+                } else {
+                    set_dev_error(a.st, DEV_UNSORTED, p);
+                }
+            }
+            const uint32_t klast = __shfl_sync(FULL, key, nvalid - 1);
+            if (lane >= nvalid) key = klast;
+            const uint32_t kprev = __shfl_up_sync(FULL, key, 1);
+            const bool head = (lane == 0) || (key != kprev);
+            const unsigned H = __ballot_sync(FULL, head);
+            const int nseg = __popc(H);
+            if (nseg == 1) {
+                const int tot = tr_reduce<V>(val, lane);
+                constexpr int L = Log2<V>::value;
+                const int k = lane >> (5 - L);
+                if ((lane & ((32 >> L) - 1)) == 0 && k < NV && tot != 0) {
+                    const int lx = (int)(key - c0) + 1 + LO;
+                    sadd(sacc, (lrow + k / NX) * SW + lx + (k % NX), tot);
+                }
+            } else if (nseg == 2) {
+                const int h2 = __ffs(H & ~1u) - 1;
+                const uint32_t k0 = __shfl_sync(FULL, key, 0);
+                const uint32_t k1 = __shfl_sync(FULL, key, h2);
+                int v2[2 * V];
+                const bool first = lane < h2;
+#pragma unroll
+                for (int i = 0; i < V; ++i) {
+                    v2[i] = first ? val[i] : 0;
+                    v2[V + i] = first ? 0 : val[i];
+                }
+                const int tot = tr_reduce<2 * V>(v2, lane);
+                constexpr int L = Log2<2 * V>::value;
+                const int k = lane >> (5 - L);
+                const int seg = k / V, kk = k % V;
+                if ((lane & ((32 >> L) - 1)) == 0 && kk < NV && tot != 0) {
+                    const int lx = (int)((seg ? k1 : k0) - c0) + 1 + LO;
+                    sadd(sacc, (lrow + kk / NX) * SW + lx + (kk % NX), tot);
+                }
+            } else {
+                const int lx = (int)(key - c0) + 1 + LO;
+#pragma unroll
+                for (int k = 0; k < NV; ++k)
+                    if (val[k] != 0) sadd(sacc, (lrow + k / NX) * SW + lx + (k % NX), val[k]);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nloc; i += DEP_THREADS) {
+        const long long v = sacc[i];
+        if (v != 0) {
+            const int ly = i / SW, lx = i % SW;
+            const int gx = wrap_i(x0 - 1 + lx, a.Nx), gy = wrap_i(y0 - 1 + ly, a.Ny);
+            atomicAdd(a.acc + (size_t)gy * a.Nx + gx, (unsigned long long)v);
+        }
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(DEP_THREADS) deposit_atomic(DepArgs a) {
+    constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
+    const float cq = charge_factor(a.st);
+    const uint32_t G = (uint32_t)a.Nx * (uint32_t)a.Ny;
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t key = __ldcs(a.cell + p);
+        if (key >= G) {
+            set_dev_error(a.st, DEV_BAD_CELL, (unsigned)p);
+            continue;
+        }
+        const int iy = (int)(key / (uint32_t)a.Nx), ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
+        int val[V];
+        if (!particle_values<S>(a, p, cq, ix, iy, val)) continue;
+#pragma unroll
+        for (int j = 0; j < NX; ++j) {
+            const size_t row = (size_t)wrap_i(iy + LO + j, a.Ny) * a.Nx;
+#pragma unroll
+            for (int i = 0; i < NX; ++i) {
+                const int v = val[j * NX + i];
+                if (v != 0)
+                    atomicAdd(a.acc + row + wrap_i(ix + LO + i, a.Nx), (unsigned long long)(long long)v);
+            }
+        }
+    }
+}
+
+// One unit of the int64 grid: inv_vol / cq (FP64).
+__global__ void fixed_unit(double inv_vol, const DevStats* st, double* unit_out) {
+    *unit_out = __ddiv_rn(inv_vol, (double)charge_factor(st));
+}
+
+__global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double background,
+                             const double* __restrict__ unitp, double* __restrict__ rho) {
+    const double unit = *unitp;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < g) rho[i] = __dadd_rn(__dmul_rn((double)acc[i], unit), background);
+}
+
+template <int S>
+static int launch_deposit(pic_ctx* c, const DepArgs& a, bool tiled) {
+    if (tiled) {
+        const size_t smem = (size_t)(a.tile_h + 3) * (a.tile_w + 3) * sizeof(long long);
+        const unsigned tiles = (unsigned)(a.tiles_x * ((c->Ny + a.tile_h - 1) / a.tile_h));
+        prof_begin(c, "deposit");
+        deposit_tiled<S><<<tiles, DEP_THREADS, smem, c->stream>>>(a);
+        prof_end(c);
+        return check_launch(c, "deposit_tiled");
+    }
+    int sms = 148;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    size_t blocks = (a.n + DEP_THREADS - 1) / DEP_THREADS;
+    const size_t cap = (size_t)sms * 16;
+    if (blocks > cap) blocks = cap;
+    if (blocks == 0) blocks = 1;
+    prof_begin(c, "deposit");
+    deposit_atomic<S><<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
+    prof_end(c);
+    return check_launch(c, "deposit_atomic");
+}
+
+int deposit_rho(pic_ctx* c, int scheme, double dt, double background) {
+    if (scheme < PIC_SCHEME_NGP || scheme > PIC_SCHEME_ESIRKEPOV) return fail(PIC_ERR_ARG, "unknown scheme");
+    bool tiled;
+    if (c->order_mode == PIC_ORDER_SORTED) {
+        if (!c->sorted) return fail(PIC_ERR_STATE, "deposit: PIC_ORDER_SORTED needs cell-sorted particles");
+        tiled = true;
+    } else if (c->order_mode == PIC_ORDER_UNSORTED) {
+        tiled = false;
+    } else {
+        tiled = c->sorted != 0;
+    }
+    PIC_CUDA_TRY(cudaMemsetAsync(c->acc, 0, c->G * sizeof(long long), c->stream));
+    DepArgs a;
+    a.cell = c->cell;
+    a.xr = c->xr;
+    a.yr = c->yr;
+    a.vx = c->vx;
+    a.vy = c->vy;
+    a.q = c->q;
+    a.offsets = c->offsets;
+    a.acc = reinterpret_cast<unsigned long long*>(c->acc);
+    a.n = c->n;
+    a.Nx = c->Nx;
+    a.Ny = c->Ny;
+    a.dtf = (float)dt;
+    a.dtdx = (float)(dt / c->dx);
+    a.dtdy = (float)(dt / c->dy);
+    a.tile_w = c->tile_w;
+    a.tile_h = c->tile_h;
+    a.tiles_x = (c->Nx + c->tile_w - 1) / c->tile_w;
+    a.st = c->dstats;
+    if (c->n > 0) {
+        switch (scheme) {
+            case PIC_SCHEME_NGP:
+                PIC_TRY(launch_deposit<S_NGP>(c, a, tiled));
+                break;
+            case PIC_SCHEME_CIC:
+                PIC_TRY(launch_deposit<S_CIC>(c, a, tiled));
+                break;
+            case PIC_SCHEME_TSC:
+                PIC_TRY(launch_deposit<S_TSC>(c, a, tiled));
+                break;
+            default:
+                PIC_TRY(launch_deposit<S_ESK>(c, a, tiled));
+                break;
+        }
+    }
+    const double inv_vol = 1.0 / (c->dx * c->dy);
+    fixed_unit<<<1, 1, 0, c->stream>>>(inv_vol, c->dstats, c->unitbuf);
+    PIC_TRY(check_launch(c, "fixed_unit"));
+    fixed_to_rho<<<(unsigned)((c->G + 255) / 256), 256, 0, c->stream>>>(c->acc, c->G, background, c->unitbuf,
+                                                                         c->rho);
+    PIC_TRY(check_launch(c, "fixed_to_rho"));
+    c->last_scheme = scheme;
+    return PIC_OK;
+}
+
+}  // namespace picgb
+
+using namespace picgb;
+
+extern "C" {
+
+int pic_gpu_set_deposit_order(pic_ctx* c, int order) {
+    if (!c) return fail(PIC_ERR_ARG, "NULL context");
+    if (order < PIC_ORDER_AUTO || order > PIC_ORDER_UNSORTED) return fail(PIC_ERR_ARG, "unknown order mode");
+    c->order_mode = order;
+    return PIC_OK;
+}
+
+int pic_gpu_set_tile(pic_ctx* c, int tile_w, int tile_h) {
+    if (!c) return fail(PIC_ERR_ARG, "NULL context");
+    if (tile_w < 1 || tile_w > 64 || tile_h < 1 || tile_h > 32)
+        return fail(PIC_ERR_ARG, "tile must be 1..64 x 1..32 cells");
+    c->tile_w = tile_w;
+    c->tile_h = tile_h;
+    return PIC_OK;
+}
+
+int pic_gpu_deposit(pic_ctx* c, int scheme, double dt, double background, double* rho_out) {
+    if (!c) return fail(PIC_ERR_ARG, "NULL context");
+    PIC_CUDA_TRY(cudaSetDevice(c->device));
+    PIC_TRY(deposit_rho(c, scheme, dt, background));
+    if (rho_out) {
+        PIC_CUDA_TRY(cudaMemcpyAsync(rho_out, c->rho, c->G * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        return pic_gpu_synchronize(c);
+    }
+    return PIC_OK;
+}
+
+int pic_gpu_get_rho_fixed(pic_ctx* c, int64_t* acc_out, double* unit_out) {
+    if (!c) return fail(PIC_ERR_ARG, "NULL context");
+    if (c->last_scheme < 0) return fail(PIC_ERR_STATE, "no deposit has run");
+    if (acc_out)
+        PIC_CUDA_TRY(cudaMemcpyAsync(acc_out, c->acc, c->G * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    if (unit_out) PIC_CUDA_TRY(cudaMemcpyAsync(unit_out, c->unitbuf, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return pic_gpu_synchronize(c);
+}
+
+int pic_gpu_get_rho(pic_ctx* c, double* rho_out) {
+    if (!c || !rho_out) return fail(PIC_ERR_ARG, "NULL argument");
+    PIC_CUDA_TRY(cudaMemcpyAsync(rho_out, c->rho, c->G * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return pic_gpu_synchronize(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,159 @@
+// Internal definitions shared by the translation units of libpicgb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "pic_gb300.h"
+
+namespace picgb {
+
+// Device-side status block. The error fields are written with atomicCAS so the
+// first failure wins; maxima of |q|, |vx|, |vy| are kept as the bit patterns of
+// non-negative floats, whose unsigned order equals their float order.
+struct DevStats {
+    unsigned int maxq_bits;
+    unsigned int maxvx_bits;
+    unsigned int maxvy_bits;
+    int err;
+    unsigned int err_info;
+    unsigned int order_breaks;  // uploads: count of i with cell[i] < cell[i-1]
+    unsigned int pad[2];
+};
+
+enum DevErr : int {
+    DEV_OK = 0,
+    DEV_BAD_POSITION = 1,   // non-finite or out-of-range position on upload
+    DEV_UNSORTED = 2,       // sorted kernel met a particle outside its row segment
+    DEV_BAD_CELL = 3,       // cell key >= Nx*Ny
+    DEV_MOVE_TOO_LARGE = 4, // trajectory longer than the general Esirkepov loop allows
+    DEV_COURANT = 5,        // Esirkepov current with |v|*dt >= cell size
+};
+
+struct ScanScratch {
+    unsigned int* partials = nullptr;  // per-level block sums
+    size_t capacity = 0;               // elements in partials
+};
+
+}  // namespace picgb
+
+struct pic_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+
+    // domain (pic::Domain, src/pic/domain.hpp)
+    double Lx = 1.0, Ly = 1.0, dx = 1.0, dy = 1.0;
+    int Nx = 1, Ny = 1;
+    size_t G = 1;
+
+    // particles, device SoA
+    size_t n = 0, cap = 0;
+    uint32_t* cell = nullptr;
+    float *xr = nullptr, *yr = nullptr, *vx = nullptr, *vy = nullptr, *q = nullptr, *m = nullptr;
+    int has_mass = 0;
+    int sorted = 0;  // particles are in stable cell order and `offsets` is valid
+
+    // sort scratch
+    uint32_t *cell_alt = nullptr, *idx_a = nullptr, *idx_b = nullptr;
+    float *alt[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    uint32_t* counts = nullptr;  // radix histograms, digit-major
+    size_t counts_cap = 0;
+    uint32_t* offsets = nullptr;  // G+1
+    uint32_t* cellcount = nullptr;  // G+1
+    picgb::ScanScratch scan;
+
+    // upload staging (device FP64)
+    double* stage = nullptr;
+    size_t stage_elems = 0;
+
+    // grid
+    long long* acc = nullptr;  // fixed-point rho accumulator (G)
+    double* rho = nullptr;     // FP64 rho (G)
+    double* unitbuf = nullptr; // device copy of the last fixed-point unit
+    int last_scheme = -1;
+
+    picgb::DevStats* dstats = nullptr;
+
+    // tuning
+    int order_mode = PIC_ORDER_AUTO;
+    int tile_w = 32, tile_h = 8;
+
+    long long launches = 0;
+
+    // optional CUDA-event records around named kernels (pic_gpu_profile_*)
+    int prof_enabled = 0;
+    struct ProfRec {
+        const char* name;
+        cudaEvent_t a, b;
+    };
+    std::vector<ProfRec>* prof = nullptr;
+};
+
+namespace picgb {
+
+// Records a failure message for pic_gpu_last_error and returns `code`.
+int fail(int code, const std::string& msg);
+// Checks a CUDA call; on failure records the message and returns PIC_ERR_CUDA.
+int cuda_fail(cudaError_t e, const char* what);
+// Reads back the device status block; maps a device error to PIC_ERR_*.
+int check_device_status(pic_ctx* ctx);
+// Launch-configuration error check after a kernel launch.
+int check_launch(pic_ctx* ctx, const char* what);
+
+void* dalloc(size_t bytes, int* rc);
+void dfree(void* p);
+
+// Device-wide exclusive scan of n u32 values in place (any n >= 0).
+int exclusive_scan_u32(pic_ctx* ctx, unsigned int* data, size_t n);
+
+// Ensures sort/offset scratch sized for the context's capacity and grid.
+int ensure_sort_scratch(pic_ctx* ctx);
+// Per-cell offsets of cell-ordered keys (histogram + scan into ctx->offsets).
+int build_offsets(pic_ctx* ctx, const uint32_t* keys);
+int sort_particles(pic_ctx* ctx);
+
+// Brackets a kernel launch with profiling events when enabled.
+void prof_begin(pic_ctx* ctx, const char* name);
+void prof_end(pic_ctx* ctx);
+
+}  // namespace picgb
+
+#define PIC_CUDA_TRY(call)                                         \
+    do {                                                           \
+        cudaError_t e__ = (call);                                  \
+        if (e__ != cudaSuccess) return picgb::cuda_fail(e__, #call); \
+    } while (0)
+
+#define PIC_TRY(expr)              \
+    do {                           \
+        int rc__ = (expr);         \
+        if (rc__ != PIC_OK) return rc__; \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+namespace picgb {
+
+__device__ __forceinline__ int wrap_i(int i, int n) {
+    int r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+__device__ __forceinline__ void set_dev_error(DevStats* st, int code, unsigned int info) {
+    if (atomicCAS(&st->err, 0, code) == 0) st->err_info = info;
+}
+
+__device__ __forceinline__ float load_maxq(const DevStats* st) { return __uint_as_float(st->maxq_bits); }
+
+// cq = 2^24 / max|q| in FP32 (IEEE division); 1 when all charges are zero.
+__device__ __forceinline__ float charge_factor(const DevStats* st) {
+    const float mq = load_maxq(st);
+    return mq > 0.0f ? __fdiv_rn(16777216.0f, mq) : 1.0f;
+}
+
+}  // namespace picgb

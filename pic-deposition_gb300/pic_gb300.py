@@ -1,0 +1,402 @@
+"""Python host binding of the GB300 PIC deposition path (ctypes over libpicgb300.so).
+
+Two layers:
+  * ``Context`` -- a thin wrapper of the C ABI in include/pic_gb300.h: device-
+    resident particles and grid, explicit upload / sort / deposit / download.
+  * Mirrors of the reference's interface (ehocine/pic-deposition,
+    src/deposition/deposition.hpp, src/pic/*.hpp): ``Domain``, ``ParticlesSoA``,
+    ``FieldGrid``, ``DepositionConfig``, ``DepositionScheme``,
+    ``DepositionBackend`` and the free functions ``depositChargeSoA``,
+    ``sortParticlesByCell``, ``particleCellIndex`` with the same names, argument
+    meaning and error behaviour (RuntimeError where the reference throws
+    std::runtime_error). The backend value ``DepositionBackend.GB300`` selects
+    this library; the reference's CPU and GPU backends are not part of it.
+
+There is no CPU fallback: importing works anywhere, but every call needs the
+compiled library and a CUDA device and raises if either is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libpicgb300.so")
+
+PIC_OK = 0
+ERRORS = {
+    -1: "PIC_ERR_ARG", -2: "PIC_ERR_CUDA", -3: "PIC_ERR_NOMEM", -4: "PIC_ERR_STATE", -5: "PIC_ERR_OVERFLOW",
+    -6: "PIC_ERR_COURANT", -7: "PIC_ERR_TIMEOUT", -8: "PIC_ERR_UNSUPPORTED", -9: "PIC_ERR_DEVICE",
+}
+ORDER_AUTO, ORDER_SORTED, ORDER_UNSORTED = 0, 1, 2
+
+
+class PicError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Domain(C.Structure):
+    _fields_ = [("Lx", C.c_double), ("Ly", C.c_double), ("Nx", C.c_int32), ("Ny", C.c_int32)]
+
+
+class _Diag(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("charge_error", "total_charge", "integrated_rho", "kinetic_energy",
+                                           "field_energy", "total_energy")]
+
+
+_lib = None
+
+# (name, restype, argtypes); restype None means int status.
+_vp = C.c_void_p
+_dp = C.POINTER(C.c_double)
+_SIGS = [
+    ("pic_gpu_create", [C.POINTER(_Domain), C.c_size_t, C.c_int, C.POINTER(_vp)]),
+    ("pic_gpu_destroy", [_vp]),
+    ("pic_gpu_synchronize", [_vp]),
+    ("pic_gpu_launch_count", [_vp, C.POINTER(C.c_longlong)]),
+    ("pic_gpu_get_stream", [_vp, C.POINTER(_vp)]),
+    ("pic_gpu_upload_particles", [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_size_t]),
+    ("pic_gpu_download_particles", [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("pic_gpu_download_device_layout", [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("pic_gpu_num_particles", [_vp, C.POINTER(C.c_size_t)]),
+    ("pic_gpu_sort", [_vp, _vp, _vp, _vp]),
+    ("pic_gpu_set_deposit_order", [_vp, C.c_int]),
+    ("pic_gpu_set_tile", [_vp, C.c_int, C.c_int]),
+    ("pic_gpu_deposit", [_vp, C.c_int, C.c_double, C.c_double, _vp]),
+    ("pic_gpu_get_rho_fixed", [_vp, _vp, _dp]),
+    ("pic_gpu_get_rho", [_vp, _vp]),
+    ("pic_gpu_is_sorted", [_vp, C.POINTER(C.c_int)]),
+    ("pic_gpu_profile_enable", [_vp, C.c_int]),
+    ("pic_gpu_profile_read", [_vp, C.c_char_p, _dp, C.POINTER(C.c_longlong)]),
+    ("pic_gpu_host_alloc", [C.c_size_t, C.POINTER(_vp)]),
+    ("pic_gpu_host_free", [_vp]),
+]
+
+
+class PinnedArray:
+    """A page-locked host buffer (pic_gpu_host_alloc) viewed as a numpy array."""
+
+    def __init__(self, n: int, dtype=np.float64):
+        dtype = np.dtype(dtype)
+        p = _vp()
+        _check(lib().pic_gpu_host_alloc(max(n, 1) * dtype.itemsize, C.byref(p)))
+        self._p = p
+        buf = (C.c_char * (max(n, 1) * dtype.itemsize)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=n)
+
+    def free(self):
+        if self._p:
+            self.array = None
+            lib().pic_gpu_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def lib():
+    """Loads libpicgb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = C.CDLL(LIB_PATH)
+        L.pic_gpu_last_error.restype = C.c_char_p
+        L.pic_gpu_last_error.argtypes = []
+        for name, args in _SIGS:
+            f = getattr(L, name, None)
+            if f is None:
+                continue
+            f.restype = C.c_int
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != PIC_OK:
+        raise PicError(rc, lib().pic_gpu_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_vp)
+
+
+def _arr(a, dt):
+    return None if a is None else np.ascontiguousarray(a, dtype=dt)
+
+
+class Context:
+    """Device-resident particles and grid on one GPU (C ABI pic_ctx)."""
+
+    def __init__(self, nx: int, ny: int, lx: float, ly: float, capacity: int, device: int = 0):
+        self.nx, self.ny, self.lx, self.ly = int(nx), int(ny), float(lx), float(ly)
+        self.G = self.nx * self.ny
+        self.capacity = int(capacity)
+        h = _vp()
+        _check(lib().pic_gpu_create(C.byref(_Domain(self.lx, self.ly, self.nx, self.ny)), self.capacity, device,
+                                    C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pic_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- particles ----
+    def upload(self, x, y, q, vx=None, vy=None, m=None):
+        arrs = [_arr(a, np.float64) for a in (x, y, vx, vy, q, m)]
+        n = len(arrs[0])
+        self._keep = arrs
+        _check(lib().pic_gpu_upload_particles(self.h, *[_ptr(a) for a in arrs], n))
+        self.n = n
+
+    def num_particles(self) -> int:
+        n = C.c_size_t()
+        _check(lib().pic_gpu_num_particles(self.h, C.byref(n)))
+        return n.value
+
+    def download(self):
+        n = self.num_particles()
+        out = [np.zeros(n) for _ in range(6)]
+        _check(lib().pic_gpu_download_particles(self.h, *[_ptr(a) for a in out]))
+        return dict(zip(("x", "y", "vx", "vy", "q", "m"), out))
+
+    def device_layout(self):
+        n = self.num_particles()
+        cell = np.zeros(n, np.uint32)
+        f = [np.zeros(n, np.float32) for _ in range(5)]
+        _check(lib().pic_gpu_download_device_layout(self.h, _ptr(cell), *[_ptr(a) for a in f]))
+        return dict(cell=cell, xr=f[0], yr=f[1], vx=f[2], vy=f[3], q=f[4])
+
+    # ---- sort ----
+    def sort(self, keys=False, perm=False, offsets=False):
+        n = self.num_particles()
+        k = np.zeros(n, np.uint32) if keys else None
+        p = np.zeros(n, np.uint32) if perm else None
+        o = np.zeros(self.G + 1, np.uint32) if offsets else None
+        _check(lib().pic_gpu_sort(self.h, _ptr(k), _ptr(p), _ptr(o)))
+        return k, p, o
+
+    # ---- deposit ----
+    def set_order(self, mode: int):
+        _check(lib().pic_gpu_set_deposit_order(self.h, mode))
+
+    def set_tile(self, w: int, h: int):
+        _check(lib().pic_gpu_set_tile(self.h, w, h))
+
+    def deposit(self, scheme: int, dt: float = 0.0, background: float = 0.0, download: bool = True):
+        rho = np.zeros(self.G) if download else None
+        _check(lib().pic_gpu_deposit(self.h, int(scheme), float(dt), float(background), _ptr(rho)))
+        return rho
+
+    def rho_fixed(self):
+        acc = np.zeros(self.G, np.int64)
+        unit = C.c_double()
+        _check(lib().pic_gpu_get_rho_fixed(self.h, _ptr(acc), C.byref(unit)))
+        return acc, unit.value
+
+    def rho(self):
+        r = np.zeros(self.G)
+        _check(lib().pic_gpu_get_rho(self.h, _ptr(r)))
+        return r
+
+    def is_sorted(self) -> bool:
+        v = C.c_int()
+        _check(lib().pic_gpu_is_sorted(self.h, C.byref(v)))
+        return bool(v.value)
+
+    def profile(self, enable: bool = True):
+        _check(lib().pic_gpu_profile_enable(self.h, int(enable)))
+
+    def profile_read(self, kernel: str):
+        """(total milliseconds, launches) of `kernel` since the last read (CUDA events on the context stream)."""
+        ms = C.c_double()
+        cnt = C.c_longlong()
+        _check(lib().pic_gpu_profile_read(self.h, kernel.encode(), C.byref(ms), C.byref(cnt)))
+        return ms.value, cnt.value
+
+    def synchronize(self):
+        _check(lib().pic_gpu_synchronize(self.h))
+
+    def launch_count(self) -> int:
+        v = C.c_longlong()
+        _check(lib().pic_gpu_launch_count(self.h, C.byref(v)))
+        return v.value
+
+    def stream(self) -> int:
+        s = _vp()
+        _check(lib().pic_gpu_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+
+# ---------------------------------------------------------------------------
+# Mirrors of the reference interface
+# ---------------------------------------------------------------------------
+class DepositionScheme(enum.IntEnum):
+    """pic::DepositionScheme, src/deposition/deposition.hpp:11."""
+    NGP = 0
+    CIC = 1
+    TSC = 2
+    Esirkepov = 3
+
+
+class DepositionBackend(enum.IntEnum):
+    """pic::DepositionBackend, src/deposition/deposition.hpp:13, plus the GB300 value."""
+    CPU = 0
+    GPUAtomics = 1
+    GPUPrivatized = 2
+    GB300 = 3
+
+
+class ParticleLayout(enum.IntEnum):
+    AoS = 0
+    SoA = 1
+
+
+@dataclass
+class Domain:
+    """pic::Domain, src/pic/domain.hpp:7-44."""
+    Lx: float = 1.0
+    Ly: float = 1.0
+    Nx: int = 64
+    Ny: int = 64
+    dt: float = 0.01
+    steps: int = 100
+
+    @property
+    def dx(self):
+        return self.Lx / self.Nx
+
+    @property
+    def dy(self):
+        return self.Ly / self.Ny
+
+    def updateDerived(self):
+        pass
+
+    def cellVolume(self):
+        return self.dx * self.dy
+
+    def domainVolume(self):
+        return self.Lx * self.Ly
+
+
+class ParticlesSoA:
+    """pic::ParticlesSoA, src/pic/particles.hpp:45-83 (host FP64 arrays)."""
+
+    def __init__(self, count: int = 0):
+        self.resize(count)
+
+    def resize(self, count: int):
+        self.x, self.y, self.vx, self.vy, self.q = (np.zeros(count) for _ in range(5))
+        self.m = np.ones(count)
+
+    def size(self) -> int:
+        return len(self.x)
+
+    def totalCharge(self) -> float:
+        return float(np.sum(self.q))
+
+    def kineticEnergy(self) -> float:
+        return float(np.sum(0.5 * self.m * (self.vx * self.vx + self.vy * self.vy)))
+
+
+class FieldGrid:
+    """pic::FieldGrid, src/pic/field_grid.hpp:9-39."""
+
+    def __init__(self, domain: Domain):
+        self._domain = domain
+        n = domain.Nx * domain.Ny
+        self.rho, self.phi, self.Ex, self.Ey = (np.zeros(n) for _ in range(4))
+
+    def domain(self):
+        return self._domain
+
+    def clearRho(self):
+        self.rho[:] = 0.0
+
+    def integratedRho(self) -> float:
+        return float(np.sum(self.rho)) * self._domain.cellVolume()
+
+    def fieldEnergy(self) -> float:
+        return 0.5 * float(np.sum(self.Ex * self.Ex + self.Ey * self.Ey)) * self._domain.cellVolume()
+
+
+@dataclass
+class DepositionConfig:
+    """pic::DepositionConfig, src/deposition/deposition.hpp:15-24."""
+    scheme: DepositionScheme = DepositionScheme.CIC
+    layout: ParticleLayout = ParticleLayout.SoA
+    backend: DepositionBackend = DepositionBackend.GB300
+    sorted: bool = False
+    num_threads: int = 1
+    dx_esirkepov: float = 0.0
+    dy_esirkepov: float = 0.0
+    esirkepov_dt: float = 0.0
+
+
+_ctx_cache: dict = {}
+
+
+def _context_for(domain: Domain, n: int) -> Context:
+    key = (domain.Nx, domain.Ny, domain.Lx, domain.Ly)
+    c = _ctx_cache.get(key)
+    if c is None or c.capacity < n:
+        if c is not None:
+            c.close()
+        c = Context(domain.Nx, domain.Ny, domain.Lx, domain.Ly, max(n, 1))
+        _ctx_cache[key] = c
+    return c
+
+
+def depositChargeSoA(particles: ParticlesSoA, grid: FieldGrid, config: DepositionConfig) -> None:
+    """pic::depositChargeSoA (src/deposition/deposition.cpp:181-200) on the GB300
+    backend: clears rho, uploads the particles, sorts them by cell when
+    ``config.sorted`` and deposits ``config.scheme`` into ``grid.rho``."""
+    if config.backend != DepositionBackend.GB300:
+        raise RuntimeError("this library implements only DepositionBackend.GB300")
+    d = grid.domain()
+    ctx = _context_for(d, particles.size())
+    ctx.upload(particles.x, particles.y, particles.q, particles.vx, particles.vy, particles.m)
+    if config.sorted:
+        ctx.sort()
+    grid.rho[:] = ctx.deposit(int(config.scheme), config.esirkepov_dt)
+
+
+def sortParticlesByCell(particles: ParticlesSoA, domain: Domain) -> None:
+    """pic::sortParticlesByCell(ParticlesSoA&, const Domain&) (src/sorting/cell_sort.cpp:22-46),
+    stable. Reorders the six host arrays in place."""
+    ctx = _context_for(domain, particles.size())
+    ctx.upload(particles.x, particles.y, particles.q, particles.vx, particles.vy, particles.m)
+    _, perm, _ = ctx.sort(perm=True)
+    for k in ("x", "y", "vx", "vy", "q", "m"):
+        setattr(particles, k, getattr(particles, k)[perm])
+
+
+def particleCellIndex(x: float, y: float, domain: Domain) -> int:
+    """pic::particleCellIndex (src/sorting/cell_sort.cpp:8-13), via the device key."""
+    ctx = _context_for(domain, 1)
+    ctx.upload(np.array([x]), np.array([y]), np.array([1.0]))
+    return int(ctx.device_layout()["cell"][0])

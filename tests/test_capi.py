@@ -1,0 +1,36 @@
+"""The C-ABI library loads and exports every symbol that include/*.h declares
+(no compute call: this runs without a GPU)."""
+import ctypes
+import glob
+import os
+import re
+
+from conftest import ROOT
+
+DECL = re.compile(r"^\s*(?:int|const char\s*\*|void)\s+(pic_gpu_\w+)\s*\(", re.M)
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        with open(h) as f:
+            names.update(DECL.findall(f.read()))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert "pic_gpu_deposit" in names and "pic_gpu_sort" in names and len(names) >= 15
+
+
+def test_library_exports_every_declared_symbol(pg):
+    lib = ctypes.CDLL(pg.LIB_PATH)
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_errors_without_device_are_status_codes(pg):
+    # a NULL context is rejected with PIC_ERR_ARG, not a crash
+    lib = pg.lib()
+    assert lib.pic_gpu_synchronize(None) == -1
+    assert b"NULL" in lib.pic_gpu_last_error()

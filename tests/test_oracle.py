@@ -1,0 +1,203 @@
+"""The CPU oracle, pinned before it is trusted.
+
+* against the reference itself (oracle/_ref, compiled from the reference
+  sources; skipped where the reference checkout is absent),
+* against the golden fixtures in tests/golden (made by the reference),
+* against the reference's archived noise study (data/benchmarks/noise_vs_grid.csv:2-13),
+* and with the reference's own test conditions (src/main_test.cpp:25-72).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+NGP, CIC, TSC, ESK = 0, 1, 2, 3
+
+
+def small():
+    return dict(np.load(os.path.join(GOLDEN, "small_32.npz")))
+
+
+# ---- against the compiled reference -------------------------------------
+@pytest.mark.parametrize("kind,args", [(0, dict(p0=1.0)), (1, dict(p0=0.01, mode=2)),
+                                       (2, dict(p0=0.05, p1=0.1, mode=1)), (3, dict(p0=0.3, p1=0.01)),
+                                       (4, dict(p0=0.2, p1=0.02))])
+def test_initialisers_bit_exact_vs_reference(port, ref, kind, args):
+    a = port.init_particles(kind, 32, 16, 1.0, 2.0, 777, seed=9, **args)
+    b = ref.init_particles(kind, 32, 16, 1.0, 2.0, 777, seed=9, **args)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("scheme", [NGP, CIC, TSC, ESK])
+@pytest.mark.parametrize("dt", [0.0, 0.01, 0.2])
+def test_deposit_bit_exact_vs_reference(port, ref, scheme, dt):
+    p = port.init_particles(0, 24, 40, 1.5, 2.5, 3000, p0=1.0, seed=5)
+    a = port.deposit_ref(24, 40, 1.5, 2.5, scheme, p, dt=dt)
+    b = ref.deposit(24, 40, 1.5, 2.5, scheme, p, dt=dt)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("scheme", [NGP, CIC, ESK])
+def test_parallel_deposit_vs_reference(port, ref, scheme):
+    # the reference merges thread grids in arrival order; equal up to FP64 rounding
+    p = port.init_particles(0, 32, 32, 1.0, 1.0, 20000, p0=1.0, seed=3)
+    a = port.deposit_ref(32, 32, 1.0, 1.0, scheme, p, dt=0.01, threads=4)
+    b = ref.deposit(32, 32, 1.0, 1.0, scheme, p, dt=0.01, threads=4)
+    assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
+
+
+def test_sort_keys_and_cells_vs_reference(port, ref):
+    p = port.init_particles(0, 20, 12, 2.0, 1.0, 5000, p0=1.0, seed=11)
+    keys, perm, offs = port.stable_cell_sort(20, 12, 2.0, 1.0, p["x"], p["y"])
+    for i in range(0, 5000, 97):
+        assert port.cell_index(20, 12, 2.0, 1.0, p["x"][i], p["y"][i]) == ref.lib.ref_cell_index(
+            20, 12, 2.0, 1.0, p["x"][i], p["y"][i])
+    r = ref.sort(20, 12, 2.0, 1.0, p)
+    rkeys = np.array([port.cell_index(20, 12, 2.0, 1.0, x, y) for x, y in zip(r["x"], r["y"])])
+    assert np.array_equal(rkeys, keys)  # same key sequence
+    # each cell holds the same multiset of particles
+    for c in range(240):
+        a = np.sort(p["x"][perm[offs[c]:offs[c + 1]]])
+        b = np.sort(r["x"][offs[c]:offs[c + 1]])
+        assert np.array_equal(a, b)
+
+
+def test_gather_push_vs_reference(port, ref):
+    p = port.init_particles(0, 16, 16, 1.0, 1.0, 2000, p0=1.0, seed=2)
+    rng = np.random.default_rng(0)
+    ex, ey = rng.normal(size=256), rng.normal(size=256)
+    a = port.gather_ref(16, 16, 1.0, 1.0, p, ex, ey, 0.05)
+    b = ref.gather(16, 16, 1.0, 1.0, p, ex, ey, 0.05)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    p["vx"] *= 30.0
+    a = port.push_ref(16, 16, 1.0, 1.0, p, 0.05)
+    b = ref.push(16, 16, 1.0, 1.0, p, 0.05)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_gs_and_fft_vs_reference(port, ref, oracle_mod):
+    g = small()
+    rho = g["poisson_rho"]
+    phi, ex, ey, _ = port.gs_ref(32, 32, 1.0, 1.0, rho, 500, 1e-6)
+    rphi, rex, rey = ref.poisson_gs(32, 32, 1.0, 1.0, rho, 500, 1e-6)
+    assert np.array_equal(phi, rphi) and np.array_equal(ex, rex)
+    fphi, fex, fey = oracle_mod.poisson_fft(32, 32, 1.0, 1.0, rho)
+    qphi, qex, qey = ref.poisson_fft(32, 32, 1.0, 1.0, rho)
+    assert np.max(np.abs(fphi - qphi)) <= 1e-12 * np.max(np.abs(qphi))
+    assert np.max(np.abs(fex - qex)) <= 1e-12 * np.max(np.abs(qex))
+
+
+# ---- against the committed golden fixtures (no reference needed) ---------
+def test_port_matches_golden_small(port):
+    g = small()
+    p = port.init_particles(0, 32, 32, 1.0, 1.0, 1000, p0=1.0, seed=123)
+    for k in ("x", "y", "q", "m"):
+        assert np.array_equal(p[k], g[k]), k
+    # velocities come from libm log/sqrt; allow the last bit across platforms
+    assert np.allclose(p["vx"], g["vx"], rtol=1e-15, atol=0)
+    for i in range(1000):
+        assert port.cell_index(32, 32, 1.0, 1.0, p["x"][i], p["y"][i]) == g["keys"][i]
+    for scheme in range(4):
+        for dt in (0.0, 0.01):
+            pp = dict(g)
+            a = port.deposit_ref(32, 32, 1.0, 1.0, scheme, dict(x=g["x"], y=g["y"], vx=g["vx"], vy=g["vy"],
+                                                                q=g["q"]), dt=dt)
+            assert np.array_equal(a, pp[f"rho_s{scheme}_dt{dt}"]), (scheme, dt)
+
+
+def test_port_matches_golden_poisson(port, oracle_mod):
+    g = small()
+    phi, ex, ey, _ = port.gs_ref(32, 32, 1.0, 1.0, g["poisson_rho"], 500, 1e-6)
+    assert np.array_equal(phi, g["gs_phi"]) and np.array_equal(ey, g["gs_ey"])
+    fphi, fex, fey = oracle_mod.poisson_fft(32, 32, 1.0, 1.0, g["poisson_rho"])
+    assert np.max(np.abs(fphi - g["fft_phi"])) <= 1e-12 * np.max(np.abs(g["fft_phi"]))
+
+
+def test_port_matches_golden_config1(port):
+    g = dict(np.load(os.path.join(GOLDEN, "config1_cic.npz")))
+    n = 1 << 20
+    p = port.init_particles(0, 256, 256, 256.0, 256.0, n, p0=1.0, seed=42)
+    assert np.array_equal(p["x"][:64], g["x_head"]) and np.array_equal(p["y"][:64], g["y_head"])
+    p["q"] = -np.ones(n)
+    rho = port.deposit_ref(256, 256, 256.0, 256.0, CIC, p)
+    assert rho.sum() == g["sum"] and (rho * rho).sum() == g["sumsq"]
+    assert np.array_equal(rho[::997], g["sample"])
+
+
+# data/benchmarks/noise_vs_grid.csv:2-13 (runNoiseVsGridStudy, src/pic/validation.cpp:445-472)
+NOISE_VS_GRID = {
+    (64, NGP): 0.6090021848, (64, CIC): 0.4003197697, (64, TSC): 0.2659117765, (64, ESK): 0.4003197697,
+    (128, NGP): 0.5826140746, (128, CIC): 0.3747387341, (128, TSC): 0.2435981661, (128, ESK): 0.3747387341,
+    (256, NGP): 0.5659049422, (256, CIC): 0.3631346553, (256, TSC): 0.2342248984, (256, ESK): 0.3631346553,
+}
+
+
+@pytest.mark.parametrize("g", [64, 128, 256])
+def test_noise_vs_grid_golden(port, oracle_mod, g):
+    p = port.init_particles(0, g, g, 1.0, 1.0, 100000, p0=1.0, seed=42)
+    for s in range(4):
+        rho = port.deposit_ref(g, g, 1.0, 1.0, s, p)
+        assert round(oracle_mod.spectral_noise(g, g, rho), 10) == NOISE_VS_GRID[(g, s)]
+
+
+# ---- the reference's own tests, on the oracle (src/main_test.cpp) ---------
+@pytest.mark.parametrize("scheme,tol", [(CIC, 1e-10), (TSC, 1e-10), (ESK, 1e-10), (NGP, 0.05)])
+def test_scheme_charge_conservation(port, scheme, tol):
+    p = port.init_particles(0, 32, 32, 1.0, 1.0, 1000, p0=1.0, seed=123)
+    rho = port.deposit_ref(32, 32, 1.0, 1.0, scheme, p, dt=0.0)
+    err = abs(port.integrated_rho(32, 32, 1.0, 1.0, rho) - p["q"].sum()) / np.abs(p["q"]).sum()
+    assert err <= tol
+
+
+def test_esirkepov_moving_charge_conservation(port):
+    p = port.init_particles(0, 32, 32, 1.0, 1.0, 1000, p0=1.0, seed=123)
+    rho = port.deposit_ref(32, 32, 1.0, 1.0, ESK, p, dt=0.01)
+    err = abs(port.integrated_rho(32, 32, 1.0, 1.0, rho) - p["q"].sum()) / np.abs(p["q"]).sum()
+    assert err <= 1e-10
+
+
+# ---- the oracle's GPU-arithmetic restatement against its FP64 restatement --
+@pytest.mark.parametrize("scheme", [NGP, CIC, TSC, ESK])
+def test_fixed_point_restatement_close_to_fp64(port, scheme):
+    p = port.init_particles(0, 64, 48, 64.0, 48.0, 50000, p0=0.04, seed=8)
+    cell, xr, yr = port.to_device(64, 48, 64.0, 48.0, p["x"], p["y"])
+    q32 = p["q"].astype(np.float32)
+    acc, unit = port.deposit_fixed(64, 48, 64.0, 48.0, scheme, cell, xr, yr, q32, p["vx"].astype(np.float32),
+                                   p["vy"].astype(np.float32), dt=0.1)
+    got = acc * unit
+    want = port.deposit_ref(64, 48, 64.0, 48.0, scheme, p, dt=0.1)
+    rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert rel < 1e-6
+    # total charge: every per-particle stencil rounds separately, so the sum is exact to 1 unit per node value
+    assert abs(acc.sum() * unit - p["q"].sum() / (1.0 * 1.0)) < 1e-3
+
+
+def test_to_device_keeps_ngp_choice(port):
+    # offsets just below 0.5 must not round up to 0.5f (ngp.cpp:116-117 uses wx >= 0.5)
+    x = np.array([0.5 - 2 ** -30, 0.5, 3.5 - 2 ** -40, 1.0 - 2 ** -30, 0.0])
+    cell, xr, yr = port.to_device(8, 8, 8.0, 8.0, x, x)
+    assert xr[0] < 0.5 and xr[1] == 0.5 and xr[2] < 0.5 and cell[2] == 3 * 8 + 3
+    assert xr[3] == 1.0  # rounds to the cell's far edge; the key stays in cell 0
+    assert cell[3] == 0
+
+
+def test_stable_sort_restatement(port):
+    rng = np.random.default_rng(1)
+    keys = rng.integers(0, 50, size=10000).astype(np.uint32)
+    ks, perm, offs = port.stable_sort_keys(keys, 50)
+    order = np.argsort(keys, kind="stable")
+    assert np.array_equal(perm, order) and np.array_equal(ks, keys[order])
+    assert np.array_equal(offs, np.concatenate([[0], np.cumsum(np.bincount(keys, minlength=50))]))
+
+
+def test_rbgs_matches_converged_lexicographic_gs(port):
+    g = small()
+    rho = g["poisson_rho"]
+    phi_rb, it, res = port.rbgs(32, 32, 1.0, 1.0, rho, tol=1e-10, max_iters=200000)
+    assert res <= 1e-10
+    phi_gs, _, _, _ = port.gs_ref(32, 32, 1.0, 1.0, rho, 200000, 1e-15)
+    phi_gs = phi_gs - phi_gs.mean()
+    assert np.max(np.abs(phi_rb - phi_gs)) <= 1e-8 * np.max(np.abs(phi_gs))
