@@ -22,11 +22,14 @@
  *    u32 cell key iy*Nx+ix; the key is computed from the FP64 host position with
  *    the reference's Domain::cellCoords (src/pic/domain.hpp:34-43), so keys are
  *    bit-identical to pic::particleCellIndex (src/sorting/cell_sort.cpp:8-13).
- *  - Charge is deposited in fixed point: each stencil contribution
- *    q*w*2^24/max|q| is rounded to the nearest integer and summed in int64, so
- *    rho is independent of summation order and bit-identical run to run. One
- *    unit of the int64 grid is inv_vol/cq, cq = (float)2^24 / max|q|
- *    (returned by pic_gpu_get_rho_fixed).
+ *  - Charge is deposited in fixed point. The resident charge is stored as
+ *    qn = q/max|q| (FP32) and a particle carries A = rint(qn*2^24) units; each
+ *    stencil value qn*2^24*w is rounded to the nearest integer, the node of
+ *    largest weight takes the remainder so the particle deposits exactly A
+ *    units, and the grid sums in int64. rho is therefore independent of
+ *    summation order, bit-identical run to run, and conserves total charge
+ *    exactly for a uniform |q|. One unit of the int64 grid is
+ *    max|q| * inv_vol * 2^-24 (returned by pic_gpu_get_rho_fixed).
  */
 #ifndef PIC_GB300_H
 #define PIC_GB300_H

@@ -84,10 +84,9 @@ class Port:
         L.orc_field_energy.argtypes = [D, _dp, _dp]
         L.orc_field_energy.restype = C.c_double
         L.orc_to_device.argtypes = [D, C.c_size_t, _dp, _dp, _u32p, _fp, _fp]
-        L.orc_fixed_charge_factor.argtypes = [C.c_size_t, _fp]
-        L.orc_fixed_charge_factor.restype = C.c_float
-        L.orc_deposit_fixed.argtypes = [D, C.c_int, C.c_size_t, _u32p, _fp, _fp, _fp, _fp, _fp, C.c_double, _i64p,
-                                        C.POINTER(C.c_double)]
+        L.orc_normalize_charge.argtypes = [C.c_size_t, _dp, _fp, C.POINTER(C.c_float)]
+        L.orc_deposit_fixed.argtypes = [D, C.c_int, C.c_size_t, _u32p, _fp, _fp, _fp, _fp, _fp, C.c_float, C.c_double,
+                                        _i64p, C.POINTER(C.c_double)]
         L.orc_fixed_to_rho.argtypes = [C.c_size_t, _i64p, C.c_double, C.c_double, _dp]
 
     @staticmethod
@@ -188,11 +187,15 @@ class Port:
         self.lib.orc_to_device(self.dom(nx, ny, lx, ly), n, _c(x, np.float64), _c(y, np.float64), cell, xr, yr)
         return cell, xr, yr
 
-    def fixed_charge_factor(self, q32):
-        q32 = _c(q32, np.float32)
-        return self.lib.orc_fixed_charge_factor(len(q32), q32)
+    def normalize_charge(self, q):
+        """(qn, maxq): the device's normalised FP32 charge and max |(float)q|."""
+        q = _c(q, np.float64)
+        qn = np.zeros(len(q), np.float32)
+        mq = C.c_float(0)
+        self.lib.orc_normalize_charge(len(q), q, qn, C.byref(mq))
+        return qn, mq.value
 
-    def deposit_fixed(self, nx, ny, lx, ly, scheme, cell, xr, yr, q32, vx32=None, vy32=None, dt=0.0):
+    def deposit_fixed(self, nx, ny, lx, ly, scheme, cell, xr, yr, qn, maxq, vx32=None, vy32=None, dt=0.0):
         n = len(cell)
         if vx32 is None:
             vx32 = np.zeros(n, np.float32)
@@ -202,7 +205,7 @@ class Port:
         unit = C.c_double(0)
         rc = self.lib.orc_deposit_fixed(self.dom(nx, ny, lx, ly), scheme, n, _c(cell, np.uint32), _c(xr, np.float32),
                                         _c(yr, np.float32), _c(vx32, np.float32), _c(vy32, np.float32),
-                                        _c(q32, np.float32), dt, acc, C.byref(unit))
+                                        _c(qn, np.float32), float(maxq), dt, acc, C.byref(unit))
         assert rc == 0
         return acc, unit.value
 

@@ -599,9 +599,14 @@ double orc_charge_error(double integrated_rho, double total_charge, double abs_c
 /* would round up to 0.5f is stored as the float just below 0.5, so the    */
 /* NGP nearest-node choice (wx >= 0.5, ngp.cpp:116-117) is kept exactly.   */
 /*                                                                          */
-/* Fixed point: cq = 2^24 / max|q| (FP32); a = q*cq. Each stencil value is  */
-/* v = (a * Y[j]) * X[i] in FP32, rounded to the nearest int32 (ties to     */
-/* even), and summed in int64. rho = acc * (inv_vol / cq) in FP64.          */
+/* Fixed point. maxq = max |(float)q|, qn = (float)q / maxq (FP32 division), */
+/* so |qn| <= 1 and a uniform |q| gives qn = +-1 exactly. a = qn * 2^24 and  */
+/* A = rint(a) is the particle's charge in units. Every frame node gets      */
+/* v = rint((a * Y[j]) * X[i]) (FP32 products, round to nearest even), then   */
+/* the node of largest weight (first maximum of X and of Y) gets              */
+/* A - (sum of the others), so a particle deposits exactly A units and the    */
+/* grid's total charge is exact. Sums are int64.                             */
+/* unit = ((double)maxq * inv_vol) * 2^-24; rho = acc * unit + background.   */
 /* ======================================================================= */
 void orc_to_device(const orc_domain* d, size_t n, const double* x, const double* y, uint32_t* cell, float* xr,
                    float* yr) {
@@ -618,13 +623,14 @@ void orc_to_device(const orc_domain* d, size_t n, const double* x, const double*
     }
 }
 
-float orc_fixed_charge_factor(size_t n, const float* q) {
+void orc_normalize_charge(size_t n, const double* q, float* qn, float* maxq_out) {
     float mq = 0.0f;
     for (size_t i = 0; i < n; ++i) {
-        const float a = fabsf(q[i]);
+        const float a = fabsf((float)q[i]);
         if (a > mq) mq = a;
     }
-    return mq > 0.0f ? 16777216.0f / mq : 1.0f;
+    for (size_t i = 0; i < n; ++i) qn[i] = mq > 0.0f ? (float)q[i] / mq : 0.0f;
+    if (maxq_out) *maxq_out = mq;
 }
 
 static inline int32_t fixed_rn(float v) { return (int32_t)lrintf(v); }
@@ -742,22 +748,29 @@ static int esk_general(float r, float dc, int* off, float* w, int cap) {
 
 #define ESK_GEN_CAP 256
 
+static int first_max(const float* X, int n) {
+    int m = 0;
+    for (int i = 1; i < n; ++i)
+        if (X[i] > X[m]) m = i;
+    return m;
+}
+
 int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t* cell, const float* xr,
-                      const float* yr, const float* vx, const float* vy, const float* q, double dt, int64_t* acc,
-                      double* unit_out) {
+                      const float* yr, const float* vx, const float* vy, const float* qn, float maxq, double dt,
+                      int64_t* acc, double* unit_out) {
     const int Nx = d->Nx, Ny = d->Ny;
     const size_t g = (size_t)Nx * Ny;
     memset(acc, 0, g * sizeof(int64_t));
-    const float cq = orc_fixed_charge_factor(n, q);
     const double inv_vol = 1.0 / (dom_dx(d) * dom_dy(d));
-    if (unit_out) *unit_out = inv_vol / (double)cq;
+    if (unit_out) *unit_out = ((double)maxq * inv_vol) * 5.9604644775390625e-08;
     const float dtf = (float)dt;
     const float dtdx = (float)(dt / dom_dx(d));
     const float dtdy = (float)(dt / dom_dy(d));
     for (size_t p = 0; p < n; ++p) {
         const int ix = (int)(cell[p] % (uint32_t)Nx);
         const int iy = (int)(cell[p] / (uint32_t)Nx);
-        const float a = q[p] * cq;
+        const float a = qn[p] * 16777216.0f;
+        const int64_t A = fixed_rn(a);
         float X[4], Y[4];
         int xlo = 0, ylo = 0, nxf = 0, nyf = 0;
         if (scheme == ORC_NGP) {
@@ -787,12 +800,20 @@ int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t*
                 } else {
                     cy = esk_general(yr[p], vy[p] * dtdy, oy, wy, ESK_GEN_CAP);
                 }
+                const int mx = first_max(wx, cx), my = first_max(wy, cy);
+                int64_t others = 0;
+                for (int j = 0; j < cy; ++j) {
+                    const float ay = a * wy[j];
+                    for (int i = 0; i < cx; ++i)
+                        if (i != mx || j != my) others += fixed_rn(ay * wx[i]);
+                }
                 for (int j = 0; j < cy; ++j) {
                     const float ay = a * wy[j];
                     const int gy = wrap_index(iy + oy[j], Ny);
                     for (int i = 0; i < cx; ++i) {
                         const int gx = wrap_index(ix + ox[i], Nx);
-                        acc[(size_t)gy * Nx + gx] += fixed_rn(ay * wx[i]);
+                        const int64_t v = (i == mx && j == my) ? A - others : (int64_t)fixed_rn(ay * wx[i]);
+                        acc[(size_t)gy * Nx + gx] += v;
                     }
                 }
                 continue;
@@ -800,12 +821,20 @@ int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t*
         } else {
             return -1;
         }
+        const int mx = first_max(X, nxf), my = first_max(Y, nyf);
+        int64_t others = 0;
+        for (int j = 0; j < nyf; ++j) {
+            const float ay = a * Y[j];
+            for (int i = 0; i < nxf; ++i)
+                if (i != mx || j != my) others += fixed_rn(ay * X[i]);
+        }
         for (int j = 0; j < nyf; ++j) {
             const float ay = a * Y[j];
             const int gy = wrap_index(iy + ylo + j, Ny);
             for (int i = 0; i < nxf; ++i) {
                 const int gx = wrap_index(ix + xlo + i, Nx);
-                acc[(size_t)gy * Nx + gx] += fixed_rn(ay * X[i]);
+                const int64_t v = (i == mx && j == my) ? A - others : (int64_t)fixed_rn(ay * X[i]);
+                acc[(size_t)gy * Nx + gx] += v;
             }
         }
     }

@@ -11,7 +11,8 @@
  *     against the reference itself (oracle/_ref, built from the reference
  *     sources) and against the reference's archived golden CSVs.
  *  2. Exact restatements of the GPU arithmetic (FP32 cell-relative positions,
- *     int32 fixed-point stencil contributions summed in int64), used for
+ *     int32 fixed-point stencil contributions summed in int64, each particle's
+ *     contributions adding up exactly to its integer charge), used for
  *     bit-exact parity of the CUDA kernels.
  *
  * Compiled with -ffp-contract=off: no multiply-add is fused, matching the CUDA
@@ -73,10 +74,10 @@ double orc_charge_error(double integrated_rho, double total_charge, double abs_c
 /* ---- restatement of the GPU data layout and fixed-point deposit ---- */
 void orc_to_device(const orc_domain* d, size_t n, const double* x, const double* y, uint32_t* cell, float* xr,
                    float* yr);
-float orc_fixed_charge_factor(size_t n, const float* q);
+void orc_normalize_charge(size_t n, const double* q, float* qn, float* maxq_out);
 int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t* cell, const float* xr,
-                      const float* yr, const float* vx, const float* vy, const float* q, double dt, int64_t* acc,
-                      double* unit_out);
+                      const float* yr, const float* vx, const float* vy, const float* qn, float maxq, double dt,
+                      int64_t* acc, double* unit_out);
 void orc_fixed_to_rho(size_t g, const int64_t* acc, double unit, double background, double* rho);
 
 #ifdef __cplusplus

@@ -270,6 +270,13 @@ __global__ void convert_particles(ConvertArgs a) {
     }
 }
 
+// q <- q / max|q| (FP32 IEEE division): a uniform |q| becomes exactly +-1.
+__global__ void normalize_charge(float* __restrict__ q, size_t n, const DevStats* st) {
+    const float mq = load_maxq(st);
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) q[i] = mq > 0.0f ? __fdiv_rn(q[i], mq) : 0.0f;
+}
+
 // Counts adjacent pairs out of cell order (0 => the upload is already sorted).
 __global__ void count_order_breaks(const uint32_t* __restrict__ cell, size_t n, DevStats* st) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -460,6 +467,10 @@ int pic_gpu_upload_particles(pic_ctx* c, const double* x, const double* y, const
     }
     c->n = n;
     c->sorted = 0;
+    if (n > 0) {
+        normalize_charge<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->q, n, c->dstats);
+        PIC_TRY(check_launch(c, "normalize_charge"));
+    }
     if (n > 1) {
         count_order_breaks<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->cell, n, c->dstats);
         PIC_TRY(check_launch(c, "count_order_breaks"));
@@ -521,6 +532,15 @@ int pic_gpu_download_particles(pic_ctx* c, double* x, double* y, double* vx, dou
     rc = fetch(c->vx, vx);
     rc = fetch(c->vy, vy);
     rc = fetch(c->q, q);
+    if (rc == PIC_OK && q) {
+        // resident charge is q / max|q|
+        DevStats st;
+        cudaError_t e = cudaMemcpy(&st, c->dstats, sizeof(st), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = cuda_fail(e, "download");
+        float mq;
+        std::memcpy(&mq, &st.maxq_bits, sizeof(float));
+        for (size_t i = 0; rc == PIC_OK && i < n; ++i) q[i] = (double)((float)q[i] * mq);
+    }
     if (rc == PIC_OK && m) {
         if (c->has_mass && c->m) {
             rc = fetch(c->m, m);

@@ -5,10 +5,14 @@
 // particle with FP64 global atomics, or one block per tile scanning all
 // particles). Design:
 //
-//  * Fixed point. Each stencil value (q*cq*Y[j])*X[i] (FP32, cq = 2^24/max|q|)
-//    is rounded to the nearest int32 and summed in int64, so the result does
-//    not depend on summation order: the tiled, atomic and oracle paths agree
-//    bit for bit. |value| <= 2^24, so a warp-wide partial sum fits in int32.
+//  * Fixed point. The resident charge is qn = q/max|q|; a particle carries
+//    A = rint(qn*2^24) units. Each stencil value (qn*2^24*Y[j])*X[i] (FP32) is
+//    rounded to the nearest int32, and the node of largest weight takes
+//    A - (sum of the others), so every particle deposits exactly A units and
+//    total charge is exact. Sums are int64, so the result does not depend on
+//    summation order: the tiled, atomic and oracle paths agree bit for bit.
+//    |value| <= 2^24 (+ a few units of remainder), so a warp-wide partial sum
+//    fits in int32.
 //  * Sorted path (deposit_tiled). One CTA per tile of tile_w x tile_h cells;
 //    its int64 accumulators (tile + halo of 1 cell below, 2 above) live in
 //    shared memory. Warp w walks rows w, w+8, ... of the tile; the particles of
@@ -192,44 +196,91 @@ struct SegIter {
     }
 };
 
-__device__ __noinline__ void esk_general_deposit(const DepArgs& a, int ix, int iy, float aq, float rx, float ry,
-                                                 float vxx, float vyy, size_t pidx) {
-    SegIter yi;
-    yi.init(ry, vyy, a.dtf, a.dtdy);
-    int oy, ox;
-    float wy, wx;
-    int ny = 0;
-    while (yi.next(oy, wy)) {
-        if (++ny > ESK_GEN_CAP) {
-            set_dev_error(a.st, DEV_MOVE_TOO_LARGE, (unsigned)pidx);
-            return;
+// Index of the first largest weight (the node that takes a particle's rounding remainder).
+template <int N>
+__device__ __forceinline__ int first_max(const float (&X)[N]) {
+    int m = 0;
+    float mv = X[0];
+#pragma unroll
+    for (int i = 1; i < N; ++i)
+        if (X[i] > mv) {
+            mv = X[i];
+            m = i;
         }
-        const float ay = aq * wy;
-        const int gy = wrap_i(iy + oy, a.Ny);
-        SegIter xi;
-        xi.init(rx, vxx, a.dtf, a.dtdx);
-        int nx = 0;
-        while (xi.next(ox, wx)) {
-            if (++nx > ESK_GEN_CAP) {
+    return m;
+}
+
+// Index of the first largest piece of a general trajectory split.
+__device__ int seg_first_max(float r, float v, float dtf, float dtd) {
+    SegIter it;
+    it.init(r, v, dtf, dtd);
+    int off, k = 0, m = 0;
+    float w, mv = -1.0f;
+    while (it.next(off, w) && k <= ESK_GEN_CAP) {
+        if (w > mv) {
+            mv = w;
+            m = k;
+        }
+        ++k;
+    }
+    return m;
+}
+
+// Moves of one cell or more: deposits straight to the global grid. The piece of
+// largest weight on each axis takes the particle's rounding remainder, as in
+// the frame path, so the particle deposits exactly A units.
+__device__ __noinline__ void esk_general_deposit(const DepArgs& a, int ix, int iy, float aq, long long A, float rx,
+                                                 float ry, float vxx, float vyy, size_t pidx) {
+    const int mx = seg_first_max(rx, vxx, a.dtf, a.dtdx);
+    const int my = seg_first_max(ry, vyy, a.dtf, a.dtdy);
+    long long others = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        SegIter yi;
+        yi.init(ry, vyy, a.dtf, a.dtdy);
+        int oy, ox, j = 0;
+        float wy, wx;
+        while (yi.next(oy, wy)) {
+            if (j >= ESK_GEN_CAP) {
                 set_dev_error(a.st, DEV_MOVE_TOO_LARGE, (unsigned)pidx);
                 return;
             }
-            const int gx = wrap_i(ix + ox, a.Nx);
-            const long long v = __float2int_rn(ay * wx);
-            if (v) atomicAdd(a.acc + (size_t)gy * a.Nx + gx, (unsigned long long)v);
+            const float ay = aq * wy;
+            const int gy = wrap_i(iy + oy, a.Ny);
+            SegIter xi;
+            xi.init(rx, vxx, a.dtf, a.dtdx);
+            int i = 0;
+            while (xi.next(ox, wx)) {
+                if (i >= ESK_GEN_CAP) {
+                    set_dev_error(a.st, DEV_MOVE_TOO_LARGE, (unsigned)pidx);
+                    return;
+                }
+                const bool major = (i == mx && j == my);
+                const long long v = major ? 0 : (long long)__float2int_rn(ay * wx);
+                if (pass == 0) {
+                    others += v;
+                } else {
+                    const long long out = major ? A - others : v;
+                    if (out) atomicAdd(a.acc + (size_t)gy * a.Nx + wrap_i(ix + ox, a.Nx), (unsigned long long)out);
+                }
+                ++i;
+            }
+            ++j;
         }
     }
 }
 
 // Stencil values of one particle into val[0 .. NX*NX) (row-major j, i), zeros
-// elsewhere. Returns false if the particle took the general Esirkepov path
-// (already deposited, val all zero).
+// elsewhere; the values add up exactly to the particle's A = rint(qn * 2^24)
+// units (the largest-weight node takes the rounding remainder). Returns false
+// if the particle took the general Esirkepov path (already deposited, val all
+// zero).
 template <int S>
-__device__ __forceinline__ bool particle_values(const DepArgs& a, size_t p, float cq, int ix, int iy,
+__device__ __forceinline__ bool particle_values(const DepArgs& a, size_t p, int ix, int iy,
                                                 int (&val)[Frame<S>::V]) {
     constexpr int NX = Frame<S>::NX, V = Frame<S>::V;
     const float rx = __ldcs(a.xr + p), ry = __ldcs(a.yr + p);
-    const float aq = __ldcs(a.q + p) * cq;
+    const float aq = __ldcs(a.q + p) * 16777216.0f;
+    const int A = __float2int_rn(aq);
     float vxx = 0.0f, vyy = 0.0f;
     if constexpr (S == S_ESK) {
         vxx = __ldcs(a.vx + p);
@@ -241,15 +292,23 @@ __device__ __forceinline__ bool particle_values(const DepArgs& a, size_t p, floa
 #pragma unroll
     for (int k = 0; k < V; ++k) val[k] = 0;
     if (!(okx && oky)) {
-        esk_general_deposit(a, ix, iy, aq, rx, ry, vxx, vyy, p);
+        esk_general_deposit(a, ix, iy, aq, A, rx, ry, vxx, vyy, p);
         return false;
     }
+    int sum = 0;
 #pragma unroll
     for (int j = 0; j < NX; ++j) {
         const float ay = aq * Y[j];
 #pragma unroll
-        for (int i = 0; i < NX; ++i) val[j * NX + i] = __float2int_rn(ay * X[i]);
+        for (int i = 0; i < NX; ++i) {
+            val[j * NX + i] = __float2int_rn(ay * X[i]);
+            sum += val[j * NX + i];
+        }
     }
+    const int kmaj = first_max(Y) * NX + first_max(X);
+    const int rem = A - sum;
+#pragma unroll
+    for (int k = 0; k < NX * NX; ++k) val[k] += (k == kmaj) ? rem : 0;
     return true;
 }
 
@@ -300,8 +359,6 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_tiled(DepArgs a) {
     const int nloc = (th + 3) * SW;
     for (int i = threadIdx.x; i < nloc; i += DEP_THREADS) sacc[i] = 0;
     __syncthreads();
-    const float cq = charge_factor(a.st);
-
     for (int r = warp; r < th; r += DEP_WARPS) {
         const int iy = y0 + r;
         const uint32_t c0 = (uint32_t)iy * (uint32_t)a.Nx + (uint32_t)x0;
@@ -318,7 +375,7 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_tiled(DepArgs a) {
                 const uint32_t k = __ldcs(a.cell + p);
                 if (k - c0 < (uint32_t)tw) {
                     key = k;
-                    particle_values<S>(a, p, cq, (int)(k - (uint32_t)iy * (uint32_t)a.Nx), iy, val);
+                    particle_values<S>(a, p, (int)(k - (uint32_t)iy * (uint32_t)a.Nx), iy, val);
                 } else {
                     set_dev_error(a.st, DEV_UNSORTED, p);
                 }
@@ -378,7 +435,6 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_tiled(DepArgs a) {
 template <int S>
 __global__ void __launch_bounds__(DEP_THREADS) deposit_atomic(DepArgs a) {
     constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
-    const float cq = charge_factor(a.st);
     const uint32_t G = (uint32_t)a.Nx * (uint32_t)a.Ny;
     for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += (size_t)gridDim.x * blockDim.x) {
         const uint32_t key = __ldcs(a.cell + p);
@@ -388,7 +444,7 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_atomic(DepArgs a) {
         }
         const int iy = (int)(key / (uint32_t)a.Nx), ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
         int val[V];
-        if (!particle_values<S>(a, p, cq, ix, iy, val)) continue;
+        if (!particle_values<S>(a, p, ix, iy, val)) continue;
 #pragma unroll
         for (int j = 0; j < NX; ++j) {
             const size_t row = (size_t)wrap_i(iy + LO + j, a.Ny) * a.Nx;
@@ -402,9 +458,9 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_atomic(DepArgs a) {
     }
 }
 
-// One unit of the int64 grid: inv_vol / cq (FP64).
+// One unit of the int64 grid (FP64).
 __global__ void fixed_unit(double inv_vol, const DevStats* st, double* unit_out) {
-    *unit_out = __ddiv_rn(inv_vol, (double)charge_factor(st));
+    *unit_out = charge_unit(st, inv_vol);
 }
 
 __global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double background,

@@ -150,10 +150,11 @@ __device__ __forceinline__ void set_dev_error(DevStats* st, int code, unsigned i
 
 __device__ __forceinline__ float load_maxq(const DevStats* st) { return __uint_as_float(st->maxq_bits); }
 
-// cq = 2^24 / max|q| in FP32 (IEEE division); 1 when all charges are zero.
-__device__ __forceinline__ float charge_factor(const DevStats* st) {
-    const float mq = load_maxq(st);
-    return mq > 0.0f ? __fdiv_rn(16777216.0f, mq) : 1.0f;
+// One unit of the int64 charge grid: max|q| * inv_vol * 2^-24 (FP64). The
+// resident charge is stored normalised, qn = q / max|q|, and a particle carries
+// rint(qn * 2^24) units.
+__device__ __forceinline__ double charge_unit(const DevStats* st, double inv_vol) {
+    return __dmul_rn(__dmul_rn((double)load_maxq(st), inv_vol), 5.9604644775390625e-08);
 }
 
 }  // namespace picgb

@@ -33,18 +33,32 @@ def gpu_deposit(pg, nx, ny, lx, ly, p, scheme, dt=0.0, order="sorted", tile=None
     return rho, acc, unit, lay
 
 
+def rel_l2(port, nx, ny, lx, ly, p, scheme, dt, rho):
+    """||rho - ref|| / ||ref||; for nearly neutral grids (||ref|| far below the
+    magnitude of the deposited charge) the magnitude ||ref(|q|)|| is the scale."""
+    ref = port.deposit_ref(nx, ny, lx, ly, scheme, p, dt=dt)
+    pa = dict(p)
+    pa["q"] = np.abs(p["q"])
+    scale = max(np.linalg.norm(ref), 1e-3 * np.linalg.norm(port.deposit_ref(nx, ny, lx, ly, scheme, pa, dt=dt)))
+    return np.linalg.norm(rho - ref) / scale if scale > 0 else 0.0
+
+
 def check(port, pg, nx, ny, lx, ly, p, scheme, dt=0.0, order="sorted", tile=None, rel_tol=REL_L2_TOL):
     rho, acc, unit, lay = gpu_deposit(pg, nx, ny, lx, ly, p, scheme, dt, order, tile)
-    want, wunit = port.deposit_fixed(nx, ny, lx, ly, scheme, lay["cell"], lay["xr"], lay["yr"], lay["q"], lay["vx"],
-                                     lay["vy"], dt)
+    cell, xr, yr = port.to_device(nx, ny, lx, ly, p["x"], p["y"])
+    qn, maxq = port.normalize_charge(p["q"])
+    if order != "sorted":
+        assert np.array_equal(lay["cell"], cell) and np.array_equal(lay["xr"], xr) and np.array_equal(lay["yr"], yr)
+        assert np.array_equal(lay["q"], qn)
+    want, wunit = port.deposit_fixed(nx, ny, lx, ly, scheme, lay["cell"], lay["xr"], lay["yr"], lay["q"], maxq,
+                                     lay["vx"], lay["vy"], dt)
     assert unit == wunit
     assert np.array_equal(acc, want), f"max |diff| {np.max(np.abs(acc - want))}"
     assert np.array_equal(rho, acc.astype(np.float64) * unit)
-    ref = port.deposit_ref(nx, ny, lx, ly, scheme, p, dt=dt)
-    nref = np.linalg.norm(ref)
-    if nref > 0:
-        rel = np.linalg.norm(rho - ref) / nref
-        assert rel <= rel_tol, rel
+    # every particle deposits exactly its integer charge
+    assert acc.sum() == int(np.sum(np.rint(qn.astype(np.float64) * 2 ** 24)))
+    rel = rel_l2(port, nx, ny, lx, ly, p, scheme, dt, rho)
+    assert rel <= rel_tol, rel
     return rho, acc
 
 
@@ -157,7 +171,8 @@ def test_bad_inputs_are_errors(pg):
         with pytest.raises(pg.PicError) as e:
             c.upload(np.array([0.1, np.nan]), np.array([0.1, 0.2]), np.array([1.0, 1.0]))
         assert e.value.code == -9
-        c.upload(np.array([0.1, 0.5]), np.array([0.1, 0.2]), np.array([1.0, 1.0]))
+        c.upload(np.array([0.5, 0.1]), np.array([0.2, 0.1]), np.array([1.0, 1.0]))  # not in cell order
+        assert not c.is_sorted()
         with pytest.raises(pg.PicError):
             c.deposit(7)
         c.set_order(pg.ORDER_SORTED)
@@ -209,8 +224,9 @@ def test_config2_full_size(port, pg, scheme):
         acc_s, unit_s = c.rho_fixed()
         lay = c.device_layout()
     assert unit == unit_s and np.array_equal(acc_u, acc_s)
+    _, maxq = port.normalize_charge(p["q"])
     want, wunit = port.deposit_fixed(1024, 1024, 1024.0, 1024.0, scheme, lay["cell"], lay["xr"], lay["yr"], lay["q"],
-                                     lay["vx"], lay["vy"], 0.1)
-    assert np.array_equal(acc_s, want)
+                                     maxq, lay["vx"], lay["vy"], 0.1)
+    assert unit == wunit and np.array_equal(acc_s, want)
     rel = np.linalg.norm(rho - ref) / np.linalg.norm(ref)
     assert rel <= REL_L2_TOL, rel

@@ -164,15 +164,16 @@ def test_esirkepov_moving_charge_conservation(port):
 def test_fixed_point_restatement_close_to_fp64(port, scheme):
     p = port.init_particles(0, 64, 48, 64.0, 48.0, 50000, p0=0.04, seed=8)
     cell, xr, yr = port.to_device(64, 48, 64.0, 48.0, p["x"], p["y"])
-    q32 = p["q"].astype(np.float32)
-    acc, unit = port.deposit_fixed(64, 48, 64.0, 48.0, scheme, cell, xr, yr, q32, p["vx"].astype(np.float32),
+    qn, maxq = port.normalize_charge(p["q"])
+    acc, unit = port.deposit_fixed(64, 48, 64.0, 48.0, scheme, cell, xr, yr, qn, maxq, p["vx"].astype(np.float32),
                                    p["vy"].astype(np.float32), dt=0.1)
     got = acc * unit
     want = port.deposit_ref(64, 48, 64.0, 48.0, scheme, p, dt=0.1)
     rel = np.linalg.norm(got - want) / np.linalg.norm(want)
     assert rel < 1e-6
-    # total charge: every per-particle stencil rounds separately, so the sum is exact to 1 unit per node value
-    assert abs(acc.sum() * unit - p["q"].sum() / (1.0 * 1.0)) < 1e-3
+    # every particle deposits exactly its integer charge, so the grid total is exact
+    assert acc.sum() == int(np.sum(np.rint(qn.astype(np.float64) * 2 ** 24)))
+    assert abs(acc.sum() * unit - p["q"].sum()) <= 1e-12 * np.abs(p["q"]).sum()
 
 
 def test_to_device_keeps_ngp_choice(port):
