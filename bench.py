@@ -42,7 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "pic-deposition_gb300"))
 
 NX = NY = 1024
-PPC = 64
+PPC = 64  # --ppc overrides (profiling runs use a smaller case)
 AMP = 0.01
 VTH = 0.1
 ESK_DT = 0.1
@@ -207,6 +207,23 @@ def make_workload(seed: int):
     import workloads
 
     return workloads.density_cos(NX, NY, PPC, AMP, VTH, seed=seed)
+
+
+def run_deposit_only(args, d: Dist):
+    """Reduced run for profilers: upload, sort, then warmup + steps deposits of
+    --scheme; prints the mean deposit-kernel time. No e2e, CPU or extra legs."""
+    import pic_gb300 as pg
+
+    p = make_workload(42)
+    n = len(p["x"])
+    with pg.Context(NX, NY, float(NX), float(NY), n) as ctx:
+        ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+        ctx.sort()
+        ctx.profile(True)
+        for _ in range(args.warmup + args.steps):
+            ctx.deposit(SCHEMES[args.scheme], ESK_DT, download=False)
+        ms, cnt = ctx.profile_read("deposit")
+    print(json.dumps({"deposit_only": args.scheme, "particles": n, "launches": cnt, "mean_kernel_ms": ms / cnt}))
 
 
 def cpu_deposit_timer(threads: int):
@@ -417,6 +434,7 @@ def run_gpu(args, d: Dist):
 
 
 def main():
+    global PPC
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4000)
@@ -425,10 +443,17 @@ def main():
     ap.add_argument("--scheme", default="CIC", choices=list(SCHEMES))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ppc", type=int, default=PPC, help="particles per cell (64 = the benchmark workload)")
+    ap.add_argument("--deposit-only", action="store_true", help="reduced run for profilers")
     args = ap.parse_args()
+    PPC = args.ppc
     if args.warmup < 3:
         args.warmup = 3
     d = Dist()
+    if args.deposit_only:
+        run_deposit_only(args, d)
+        d.close()
+        return
     try:
         res = run_reference(args, d) if args.impl == "reference" else run_gpu(args, d)
     finally:
