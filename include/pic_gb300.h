@@ -149,6 +149,33 @@ int pic_gpu_deposit(pic_ctx* ctx, int scheme, double dt, double background, doub
 int pic_gpu_get_rho_fixed(pic_ctx* ctx, int64_t* acc_out, double* unit_out);
 int pic_gpu_get_rho(pic_ctx* ctx, double* rho_out);
 
+/* ---- deposit for callers that cannot allocate device memory ----
+ *
+ * No counterpart in the reference: it exists for hosts that own the whole
+ * device-memory budget (a particle code that fills the GPU from its own pool)
+ * or that must not pay the device-wide synchronisation of cudaMalloc/cudaFree
+ * inside their time-step loop. It needs no context and allocates nothing: the
+ * caller passes device arrays in this library's particle layout (cell key
+ * iy*Nx+ix, in-cell offsets xr, yr in [0,1], charge qn = q/max_abs_q) and a
+ * device output grid rho of Nx*Ny doubles; the int64 scratch grid lives in a
+ * fixed device array of PIC_NOALLOC_MAX_CELLS cells (8 MiB) that every GPU
+ * loading this library holds until the process exits.
+ *  - Grids above PIC_NOALLOC_MAX_CELLS cells are rejected with PIC_ERR_ARG.
+ *  - Schemes NGP, CIC and TSC; the result equals pic_gpu_deposit's bit for bit
+ *    on the same particles. Particles whose key is not below Nx*Ny are skipped.
+ *  - The first call on a device looks up the scratch array's device address
+ *    (once per device, with that device current); make that first call before
+ *    any stream capture.
+ *  - All calls share the one scratch array, which keeps the last call's sums;
+ *    each call clears the part it uses. Calls whose work overlaps on the GPU
+ *    (different streams or host threads) race and corrupt each other.
+ *  - Work is queued on `stream` (a cudaStream_t; NULL = the default stream);
+ *    the call does not synchronise. */
+#define PIC_NOALLOC_MAX_CELLS (1024 * 1024)
+int pic_gpu_deposit_noalloc(const pic_domain* domain, int scheme, const uint32_t* cell, const float* xr,
+                            const float* yr, const float* qn, size_t n, float max_abs_q, double background,
+                            double* rho, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
