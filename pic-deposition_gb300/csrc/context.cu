@@ -329,7 +329,7 @@ int pic_gpu_create(const pic_domain* dom, size_t capacity, int device, pic_ctx**
         delete c;
         return cuda_fail(e, "cudaStreamCreate");
     }
-    const size_t cp = capacity ? capacity : 1;
+    const size_t cp = (capacity ? capacity : 1) + PARTICLE_PAD;
     c->cell = (uint32_t*)A(cp * 4);
     c->xr = (float*)A(cp * 4);
     c->yr = (float*)A(cp * 4);
@@ -411,7 +411,7 @@ int pic_gpu_upload_particles(pic_ctx* c, const double* x, const double* y, const
     }
     if (need_m && !c->m) {
         int rc;
-        c->m = (float*)dalloc((c->cap ? c->cap : 1) * 4, &rc);
+        c->m = (float*)dalloc(((c->cap ? c->cap : 1) + PARTICLE_PAD) * 4, &rc);
         if (!c->m) return rc;
     }
     c->has_mass = need_m ? 1 : 0;

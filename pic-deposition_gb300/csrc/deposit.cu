@@ -275,17 +275,11 @@ __device__ __noinline__ void esk_general_deposit(const DepArgs& a, int ix, int i
 // if the particle took the general Esirkepov path (already deposited, val all
 // zero).
 template <int S>
-__device__ __forceinline__ bool particle_values(const DepArgs& a, size_t p, int ix, int iy,
-                                                int (&val)[Frame<S>::V]) {
+__device__ __forceinline__ bool stencil_values(const DepArgs& a, float rx, float ry, float qn, float vxx, float vyy,
+                                               int ix, int iy, size_t p, int (&val)[Frame<S>::V]) {
     constexpr int NX = Frame<S>::NX, V = Frame<S>::V;
-    const float rx = __ldcs(a.xr + p), ry = __ldcs(a.yr + p);
-    const float aq = __ldcs(a.q + p) * 16777216.0f;
+    const float aq = qn * 16777216.0f;
     const int A = __float2int_rn(aq);
-    float vxx = 0.0f, vyy = 0.0f;
-    if constexpr (S == S_ESK) {
-        vxx = __ldcs(a.vx + p);
-        vyy = __ldcs(a.vy + p);
-    }
     float X[NX], Y[NX];
     const bool okx = axis_frame<S>(rx, vxx, a.dtf, a.dtdx, X);
     const bool oky = axis_frame<S>(ry, vyy, a.dtf, a.dtdy, Y);
@@ -312,40 +306,58 @@ __device__ __forceinline__ bool particle_values(const DepArgs& a, size_t p, int 
     return true;
 }
 
-// Transposed warp reduction of V int values per lane (V a power of two <= 32).
-// Afterwards every lane holds the warp total of value index lane >> (5 - log2 V)
-// in v[0]; the 32/V lanes that share an index hold the same total.
-template <int V>
-__device__ __forceinline__ int tr_reduce(int (&v)[V], int lane) {
-    constexpr int L = (V >= 32) ? 5 : (V >= 16) ? 4 : (V >= 8) ? 3 : (V >= 4) ? 2 : (V >= 2) ? 1 : 0;
-#pragma unroll
-    for (int s = 0; s < 5; ++s) {
-        const int off = 16 >> s;
-        if (s < L) {
-            const int half = V >> (s + 1);
-            const bool upper = (lane & off) != 0;
-#pragma unroll
-            for (int i = 0; i < half; ++i) {
-                const int send = upper ? v[i] : v[i + half];
-                const int keep = upper ? v[i + half] : v[i];
-                v[i] = keep + __shfl_xor_sync(FULL, send, off);
-            }
-        } else {
-            v[0] += __shfl_xor_sync(FULL, v[0], off);
-        }
+template <int S>
+__device__ __forceinline__ bool particle_values(const DepArgs& a, size_t p, int ix, int iy,
+                                                int (&val)[Frame<S>::V]) {
+    const float rx = __ldcs(a.xr + p), ry = __ldcs(a.yr + p);
+    const float qn = __ldcs(a.q + p);
+    float vxx = 0.0f, vyy = 0.0f;
+    if constexpr (S == S_ESK) {
+        vxx = __ldcs(a.vx + p);
+        vyy = __ldcs(a.vy + p);
     }
-    return v[0];
+    return stencil_values<S>(a, rx, ry, qn, vxx, vyy, ix, iy, p, val);
 }
-
-template <int V>
-struct Log2 {
-    static constexpr int value = (V >= 32) ? 5 : (V >= 16) ? 4 : (V >= 8) ? 3 : (V >= 4) ? 2 : (V >= 2) ? 1 : 0;
-};
 
 __device__ __forceinline__ void sadd(long long* s, int idx, int v) {
     atomicAdd(reinterpret_cast<unsigned long long*>(s + idx), (unsigned long long)(long long)v);
 }
 
+constexpr uint32_t NO_CELL = 0xffffffffu;
+
+// Four consecutive particles of each field, one 128-bit streaming load per field.
+template <int S>
+struct Quad {
+    uint4 cell;
+    float4 xr, yr, q, vx, vy;
+};
+
+template <int S>
+__device__ __forceinline__ void load_quad(const DepArgs& a, uint32_t p0, bool ok, Quad<S>& d) {
+    if (ok) {
+        d.cell = __ldcs(reinterpret_cast<const uint4*>(a.cell + p0));
+        d.xr = __ldcs(reinterpret_cast<const float4*>(a.xr + p0));
+        d.yr = __ldcs(reinterpret_cast<const float4*>(a.yr + p0));
+        d.q = __ldcs(reinterpret_cast<const float4*>(a.q + p0));
+        if constexpr (S == S_ESK) {
+            d.vx = __ldcs(reinterpret_cast<const float4*>(a.vx + p0));
+            d.vy = __ldcs(reinterpret_cast<const float4*>(a.vy + p0));
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t u4(const uint4& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+__device__ __forceinline__ float f4(const float4& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+
+// Sorted path. See the file header: one CTA per tile, one warp per tile row at
+// a time; each warp step covers 128 particles (4 consecutive per lane, loaded
+// with one 128-bit load per field, the next step's loads issued before this
+// step's arithmetic). A lane sums its particles' stencil values in registers
+// while they share a cell (writing to shared memory only when its cell
+// changes); then a segmented warp scan over the lanes' (cell, sums) leaves each
+// run of equal cells' total in the run's last lane, which adds it to the tile's
+// shared int64 accumulators. The scan is correct for any order of cells; the
+// sortedness only makes runs long.
 template <int S>
 __global__ void __launch_bounds__(DEP_THREADS) deposit_tiled(DepArgs a) {
     constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
@@ -359,66 +371,80 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_tiled(DepArgs a) {
     const int nloc = (th + 3) * SW;
     for (int i = threadIdx.x; i < nloc; i += DEP_THREADS) sacc[i] = 0;
     __syncthreads();
+    const unsigned upto = (lane == 31) ? FULL : ((2u << lane) - 1u);
     for (int r = warp; r < th; r += DEP_WARPS) {
         const int iy = y0 + r;
-        const uint32_t c0 = (uint32_t)iy * (uint32_t)a.Nx + (uint32_t)x0;
+        const uint32_t rowbase = (uint32_t)iy * (uint32_t)a.Nx;
+        const uint32_t c0 = rowbase + (uint32_t)x0;
         const uint32_t pbeg = a.offsets[c0], pend = a.offsets[c0 + tw];
-        const int lrow = r + 1 + LO;  // local row of frame row 0
-        for (uint32_t base = pbeg; base < pend; base += 32) {
-            const uint32_t p = base + lane;
-            const int nvalid = (int)min(pend - base, 32u);
-            int val[V];
+        const int lrow = r + 1 + LO;               // local row of frame row 0
+        const int lcol = 1 + LO - x0;              // local column of frame column 0 is ix + lcol
+        uint32_t base = pbeg & ~3u;
+        Quad<S> cur, nxt;
+        load_quad<S>(a, base + 4u * lane, base + 4u * lane < pend, cur);
+        while (base < pend) {
+            const uint32_t nbase = base + 128u;
+            if (nbase < pend) load_quad<S>(a, nbase + 4u * lane, nbase + 4u * lane < pend, nxt);
+            uint32_t ckey = NO_CELL;
+            int acc[NV];
 #pragma unroll
-            for (int k = 0; k < V; ++k) val[k] = 0;
-            uint32_t key = c0;
-            if (lane < nvalid) {
-                const uint32_t k = __ldcs(a.cell + p);
-                if (k - c0 < (uint32_t)tw) {
-                    key = k;
-                    particle_values<S>(a, p, (int)(k - (uint32_t)iy * (uint32_t)a.Nx), iy, val);
-                } else {
-                    set_dev_error(a.st, DEV_UNSORTED, p);
+            for (int k = 0; k < NV; ++k) acc[k] = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t p = base + 4u * lane + (uint32_t)k;
+                if (p >= pbeg && p < pend) {
+                    const uint32_t key = u4(cur.cell, k);
+                    if (key - c0 >= (uint32_t)tw) {
+                        set_dev_error(a.st, DEV_UNSORTED, p);
+                        continue;
+                    }
+                    int val[V];
+                    float vxx = 0.0f, vyy = 0.0f;
+                    if constexpr (S == S_ESK) {
+                        vxx = f4(cur.vx, k);
+                        vyy = f4(cur.vy, k);
+                    }
+                    if (!stencil_values<S>(a, f4(cur.xr, k), f4(cur.yr, k), f4(cur.q, k), vxx, vyy,
+                                           (int)(key - rowbase), iy, p, val))
+                        continue;
+                    if (key != ckey) {
+                        if (ckey != NO_CELL) {
+                            const int lx = (int)(ckey - rowbase) + lcol;
+#pragma unroll
+                            for (int q = 0; q < NV; ++q)
+                                if (acc[q] != 0) sadd(sacc, (lrow + q / NX) * SW + lx + (q % NX), acc[q]);
+                        }
+                        ckey = key;
+#pragma unroll
+                        for (int q = 0; q < NV; ++q) acc[q] = val[q];
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < NV; ++q) acc[q] += val[q];
+                    }
                 }
             }
-            const uint32_t klast = __shfl_sync(FULL, key, nvalid - 1);
-            if (lane >= nvalid) key = klast;
-            const uint32_t kprev = __shfl_up_sync(FULL, key, 1);
-            const bool head = (lane == 0) || (key != kprev);
-            const unsigned H = __ballot_sync(FULL, head);
-            const int nseg = __popc(H);
-            if (nseg == 1) {
-                const int tot = tr_reduce<V>(val, lane);
-                constexpr int L = Log2<V>::value;
-                const int k = lane >> (5 - L);
-                if ((lane & ((32 >> L) - 1)) == 0 && k < NV && tot != 0) {
-                    const int lx = (int)(key - c0) + 1 + LO;
-                    sadd(sacc, (lrow + k / NX) * SW + lx + (k % NX), tot);
-                }
-            } else if (nseg == 2) {
-                const int h2 = __ffs(H & ~1u) - 1;
-                const uint32_t k0 = __shfl_sync(FULL, key, 0);
-                const uint32_t k1 = __shfl_sync(FULL, key, h2);
-                int v2[2 * V];
-                const bool first = lane < h2;
+            // segmented inclusive scan over lanes: runs of equal ckey
+            const uint32_t kprev = __shfl_up_sync(FULL, ckey, 1);
+            const unsigned H = __ballot_sync(FULL, lane == 0 || ckey != kprev);
+            const int segstart = 31 - __clz(H & upto);
 #pragma unroll
-                for (int i = 0; i < V; ++i) {
-                    v2[i] = first ? val[i] : 0;
-                    v2[V + i] = first ? 0 : val[i];
-                }
-                const int tot = tr_reduce<2 * V>(v2, lane);
-                constexpr int L = Log2<2 * V>::value;
-                const int k = lane >> (5 - L);
-                const int seg = k / V, kk = k % V;
-                if ((lane & ((32 >> L) - 1)) == 0 && kk < NV && tot != 0) {
-                    const int lx = (int)((seg ? k1 : k0) - c0) + 1 + LO;
-                    sadd(sacc, (lrow + kk / NX) * SW + lx + (kk % NX), tot);
-                }
-            } else {
-                const int lx = (int)(key - c0) + 1 + LO;
+            for (int d = 1; d < 32; d <<= 1) {
+                const bool take = lane - d >= segstart;
 #pragma unroll
-                for (int k = 0; k < NV; ++k)
-                    if (val[k] != 0) sadd(sacc, (lrow + k / NX) * SW + lx + (k % NX), val[k]);
+                for (int q = 0; q < NV; ++q) {
+                    const int o = __shfl_up_sync(FULL, acc[q], d);
+                    if (take) acc[q] += o;
+                }
             }
+            const bool tail = (lane == 31) || ((H >> (lane + 1)) & 1u);
+            if (tail && ckey != NO_CELL) {
+                const int lx = (int)(ckey - rowbase) + lcol;
+#pragma unroll
+                for (int q = 0; q < NV; ++q)
+                    if (acc[q] != 0) sadd(sacc, (lrow + q / NX) * SW + lx + (q % NX), acc[q]);
+            }
+            cur = nxt;
+            base = nbase;
         }
     }
     __syncthreads();

@@ -34,6 +34,11 @@ enum DevErr : int {
     DEV_COURANT = 5,        // Esirkepov current with |v|*dt >= cell size
 };
 
+// Particle arrays are allocated this many elements longer than the capacity:
+// the sorted deposit reads four consecutive particles with one 128-bit load
+// from a 4-aligned index below n, which may reach up to 3 elements past n.
+constexpr size_t PARTICLE_PAD = 32;
+
 struct ScanScratch {
     unsigned int* partials = nullptr;  // per-level block sums
     size_t capacity = 0;               // elements in partials

@@ -185,7 +185,7 @@ __global__ void cell_histogram(const uint32_t* __restrict__ keys, size_t n, uint
 }
 
 int ensure_sort_scratch(pic_ctx* c) {
-    const size_t cp = c->cap ? c->cap : 1;
+    const size_t cp = (c->cap ? c->cap : 1) + PARTICLE_PAD;
     int rc = PIC_OK;
     if (!c->cell_alt) c->cell_alt = (uint32_t*)dalloc(cp * 4, &rc);
     if (rc) return rc;
