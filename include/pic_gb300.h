@@ -149,6 +149,32 @@ int pic_gpu_deposit(pic_ctx* ctx, int scheme, double dt, double background, doub
 int pic_gpu_get_rho_fixed(pic_ctx* ctx, int64_t* acc_out, double* unit_out);
 int pic_gpu_get_rho(pic_ctx* ctx, double* rho_out);
 
+/* ---- fields: pic::FieldGrid (src/pic/field_grid.hpp:9-39) ---- */
+
+/* Replaces FieldGrid::rho() with caller data (Nx*Ny doubles). */
+int pic_gpu_set_rho(pic_ctx* ctx, const double* rho);
+/* Sets phi, Ex, Ey (any may be NULL) and refreshes the FP32 copies the gather reads. */
+int pic_gpu_set_fields(pic_ctx* ctx, const double* phi, const double* Ex, const double* Ey);
+int pic_gpu_get_fields(pic_ctx* ctx, double* phi, double* Ex, double* Ey);
+
+/* ---- Poisson: replaces pic::PoissonSolverFFT::solve (src/pic/poisson_fft.cpp:45-94) ----
+ * phi = IFFT(FFT(rho*dV) / k^2) with the continuous k^2 and DC set to 0, then
+ * E = -(phi[i+1]-phi[i])/dx. FP64 cuFFT (D2Z/Z2D) plus this library's kernels. */
+int pic_gpu_poisson_fft(pic_ctx* ctx);
+
+/* ---- particle motion ---- */
+
+/* pic::gatherFieldsSoA (src/deposition/deposition.cpp:335-356): v += -(q/m)*E*dt. */
+int pic_gpu_gather(pic_ctx* ctx, double dt);
+/* pic::pushParticlesSoA (deposition.cpp:367-374): x += v*dt, periodic wrap. Marks particles unsorted. */
+int pic_gpu_push(pic_ctx* ctx, double dt);
+/* gather then push in one pass over the particles (44 B per particle). */
+int pic_gpu_gather_push(pic_ctx* ctx, double dt);
+
+/* ---- diagnostics: pic::computeDiagnostics (src/pic/diagnostics.cpp:42-51), FP64 sums
+ *      in a fixed order (bit-identical run to run) ---- */
+int pic_gpu_diagnostics(pic_ctx* ctx, pic_diag* out);
+
 /* ---- deposit for callers that cannot allocate device memory ----
  *
  * No counterpart in the reference: it exists for hosts that own the whole

@@ -88,6 +88,8 @@ class Port:
         L.orc_deposit_fixed.argtypes = [D, C.c_int, C.c_size_t, _u32p, _fp, _fp, _fp, _fp, _fp, C.c_float, C.c_double,
                                         _i64p, C.POINTER(C.c_double)]
         L.orc_fixed_to_rho.argtypes = [C.c_size_t, _i64p, C.c_double, C.c_double, _dp]
+        L.orc_move_f32.argtypes = [D, C.c_size_t, _u32p, _fp, _fp, _fp, _fp, _fp, C.c_float, C.c_void_p, _dp, _dp,
+                                   C.c_double, C.c_int, C.c_int]
 
     @staticmethod
     def dom(nx, ny, lx, ly):
@@ -208,6 +210,16 @@ class Port:
                                         _c(qn, np.float32), float(maxq), dt, acc, C.byref(unit))
         assert rc == 0
         return acc, unit.value
+
+    def move_f32(self, nx, ny, lx, ly, lay, maxq, ex, ey, dt, gather=True, push=True, m=None):
+        """The GPU's FP32 gather/push on a copy of the device layout `lay`."""
+        out = {k: _c(lay[k], np.uint32 if k == "cell" else np.float32).copy() for k in ("cell", "xr", "yr", "vx", "vy")}
+        mm = None if m is None else _c(m, np.float32)
+        self.lib.orc_move_f32(self.dom(nx, ny, lx, ly), len(out["cell"]), out["cell"], out["xr"], out["yr"], out["vx"],
+                              out["vy"], _c(lay["q"], np.float32), float(maxq),
+                              None if mm is None else mm.ctypes.data_as(C.c_void_p), _c(ex, np.float64),
+                              _c(ey, np.float64), dt, int(gather), int(push))
+        return out
 
     @staticmethod
     def fixed_to_rho(acc, unit, background=0.0):

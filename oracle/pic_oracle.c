@@ -844,3 +844,54 @@ int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t*
 void orc_fixed_to_rho(size_t g, const int64_t* acc, double unit, double background, double* rho) {
     for (size_t i = 0; i < g; ++i) rho[i] = (double)acc[i] * unit + background;
 }
+
+/* ======================================================================= */
+/* Restatement of the GPU's cell-relative FP32 gather / push               */
+/* (gatherFieldsSoA / pushParticlesSoA, deposition.cpp:335-374, in the      */
+/* device layout): E is read as FP32 copies of the FP64 fields,            */
+/*   e = ((E00*(1-wx))*(1-wy) + (E10*wx)*(1-wy)) + (E01*(1-wx))*wy + (E11*wx)*wy */
+/*   v = v + ((-q/m)*e)*dt,   r' = r + v*dt/dx, cell moves by floor(r').    */
+/* ======================================================================= */
+void orc_move_f32(const orc_domain* d, size_t n, uint32_t* cell, float* xr, float* yr, float* vx, float* vy,
+                  const float* qn, float maxq, const float* m, const double* Ex, const double* Ey, double dt,
+                  int gather, int push) {
+    const int Nx = d->Nx, Ny = d->Ny;
+    const float dtf = (float)dt;
+    const float dtdx = (float)(dt / dom_dx(d));
+    const float dtdy = (float)(dt / dom_dy(d));
+    for (size_t p = 0; p < n; ++p) {
+        int iy = (int)(cell[p] / (uint32_t)Nx);
+        int ix = (int)(cell[p] - (uint32_t)iy * (uint32_t)Nx);
+        float rx = xr[p], ry = yr[p];
+        float vxx = vx[p], vyy = vy[p];
+        if (gather) {
+            const int ixp = (ix + 1) % Nx, iyp = (iy + 1) % Ny;
+            const size_t i00 = (size_t)iy * Nx + ix, i10 = (size_t)iy * Nx + ixp;
+            const size_t i01 = (size_t)iyp * Nx + ix, i11 = (size_t)iyp * Nx + ixp;
+            const float omx = 1.0f - rx, omy = 1.0f - ry;
+            const float ex = ((((float)Ex[i00] * omx) * omy + ((float)Ex[i10] * rx) * omy) +
+                              ((float)Ex[i01] * omx) * ry) + ((float)Ex[i11] * rx) * ry;
+            const float ey = ((((float)Ey[i00] * omx) * omy + ((float)Ey[i10] * rx) * omy) +
+                              ((float)Ey[i01] * omx) * ry) + ((float)Ey[i11] * rx) * ry;
+            const float qf = qn[p] * maxq;
+            const float coef = m ? (-qf) / m[p] : -qf;
+            vxx = vxx + (coef * ex) * dtf;
+            vyy = vyy + (coef * ey) * dtf;
+            vx[p] = vxx;
+            vy[p] = vyy;
+        }
+        if (push) {
+            float x = rx + vxx * dtdx;
+            float s = floorf(x);
+            rx = x - s;
+            ix = wrap_index(ix + (int)s, Nx);
+            x = ry + vyy * dtdy;
+            s = floorf(x);
+            ry = x - s;
+            iy = wrap_index(iy + (int)s, Ny);
+            xr[p] = rx;
+            yr[p] = ry;
+            cell[p] = (uint32_t)iy * (uint32_t)Nx + (uint32_t)ix;
+        }
+    }
+}

@@ -79,6 +79,9 @@ int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t*
                       const float* yr, const float* vx, const float* vy, const float* qn, float maxq, double dt,
                       int64_t* acc, double* unit_out);
 void orc_fixed_to_rho(size_t g, const int64_t* acc, double unit, double background, double* rho);
+void orc_move_f32(const orc_domain* d, size_t n, uint32_t* cell, float* xr, float* yr, float* vx, float* vy,
+                  const float* qn, float maxq, const float* m, const double* Ex, const double* Ey, double dt,
+                  int gather, int push);
 
 #ifdef __cplusplus
 }

@@ -364,6 +364,7 @@ int pic_gpu_destroy(pic_ctx* c) {
                     c->alt[0], c->alt[1], c->alt[2], c->alt[3], c->alt[4], c->alt[5], c->counts, c->offsets,
                     c->cellcount, c->scan.partials, c->stage, c->acc, c->rho, c->unitbuf, c->dstats};
     for (void* p : ptrs) dfree(p);
+    release_fields(c);
     prof_clear(c, nullptr);
     delete c->prof;
     if (c->stream) cudaStreamDestroy(c->stream);

@@ -81,6 +81,18 @@ struct pic_ctx {
     double* unitbuf = nullptr; // device copy of the last fixed-point unit
     int last_scheme = -1;
 
+    // fields (FieldGrid phi/Ex/Ey, src/pic/field_grid.hpp) + FP32 copies for the gather
+    double *phi = nullptr, *Ex = nullptr, *Ey = nullptr;
+    float *Exf = nullptr, *Eyf = nullptr;
+    int fields_init = 0;
+    // cuFFT Poisson
+    void* spec = nullptr;  // Ny x (Nx/2+1) complex
+    double* fft_rhs = nullptr;
+    int fft_fwd = 0, fft_inv = 0, fft_ready = 0;
+    // deterministic FP64 reductions
+    double* red_partials = nullptr;
+    double* red_out = nullptr;
+
     picgb::DevStats* dstats = nullptr;
 
     // tuning
@@ -120,6 +132,16 @@ int ensure_sort_scratch(pic_ctx* ctx);
 // Per-cell offsets of cell-ordered keys (histogram + scan into ctx->offsets).
 int build_offsets(pic_ctx* ctx, const uint32_t* keys);
 int sort_particles(pic_ctx* ctx);
+
+// Fields, Poisson and diagnostics (fields.cu).
+int ensure_fields(pic_ctx* ctx);
+int poisson_fft(pic_ctx* ctx);
+int efield_from_phi(pic_ctx* ctx);
+int diagnostics_async(pic_ctx* ctx);
+int read_diagnostics(pic_ctx* ctx, pic_diag* d);
+void release_fields(pic_ctx* ctx);
+// Deposit (deposit.cu).
+int deposit_rho(pic_ctx* ctx, int scheme, double dt, double background);
 
 // Brackets a kernel launch with profiling events when enabled.
 void prof_begin(pic_ctx* ctx, const char* name);

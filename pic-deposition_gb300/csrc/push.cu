@@ -1,0 +1,144 @@
+// Field gather and leapfrog push on the resident particles.
+//
+//  gather   = pic::gatherFieldsSoA (src/deposition/deposition.cpp:335-356): CIC
+//             interpolation of Ex, Ey at the particle with the deposit's
+//             weights, then v += -(q/m) * E * dt.
+//  push     = pic::pushParticlesSoA (deposition.cpp:367-374): x += v * dt with
+//             periodic wrap (Domain::wrapPosition, src/pic/domain.hpp:27-32).
+//  fused    = gather then push in one pass over the particles (kick of step n
+//             and drift of step n+1 in the reference's loop order,
+//             src/pic/simulation.cpp:82-131): reads cell, offsets, v, q
+//             (24 B) and writes cell, offsets, v (20 B) per particle.
+//
+// Positions stay cell-relative in FP32: r' = r + v*dt/dx, the integer part moves
+// the cell key (wrapped) and the fraction stays in [0,1]. Operation order
+// follows the reference:
+//   e  = ((E00*(1-wx))*(1-wy) + (E10*wx)*(1-wy)) + (E01*(1-wx))*wy + (E11*wx)*wy
+//   v  = v + ((-q/m)*e)*dt
+// with E the FP32 copies of the FP64 fields. Compiled with --fmad=false, so the
+// oracle reproduces every bit.
+#include "pic_internal.cuh"
+
+namespace picgb {
+
+struct MoveArgs {
+    uint32_t* cell;
+    float *xr, *yr, *vx, *vy;
+    const float* q;
+    const float* m;  // null when every mass is 1
+    const float* Exf;
+    const float* Eyf;
+    size_t n;
+    int Nx, Ny;
+    float dtf, dtdx, dtdy;
+    const DevStats* st;
+};
+
+__device__ __forceinline__ float interp(const float* __restrict__ E, size_t i00, size_t i10, size_t i01, size_t i11,
+                                        float wx, float wy) {
+    const float omx = 1.0f - wx, omy = 1.0f - wy;
+    return (((__ldg(E + i00) * omx) * omy + (__ldg(E + i10) * wx) * omy) + (__ldg(E + i01) * omx) * wy) +
+           (__ldg(E + i11) * wx) * wy;
+}
+
+__device__ __forceinline__ void drift(float& r, int& i, float v, float dtd, int n) {
+    const float x = r + v * dtd;
+    const float s = floorf(x);
+    r = x - s;
+    i = wrap_i(i + (int)s, n);
+}
+
+template <bool GATHER, bool PUSH>
+__global__ void __launch_bounds__(256) move_particles(MoveArgs a) {
+    const float maxq = load_maxq(a.st);
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t key = a.cell[p];
+        int iy = (int)(key / (uint32_t)a.Nx);
+        int ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
+        float rx = a.xr[p], ry = a.yr[p];
+        float vxx = a.vx[p], vyy = a.vy[p];
+        if constexpr (GATHER) {
+            const int ixp = (ix + 1) % a.Nx, iyp = (iy + 1) % a.Ny;
+            const size_t i00 = (size_t)iy * a.Nx + ix, i10 = (size_t)iy * a.Nx + ixp;
+            const size_t i01 = (size_t)iyp * a.Nx + ix, i11 = (size_t)iyp * a.Nx + ixp;
+            const float ex = interp(a.Exf, i00, i10, i01, i11, rx, ry);
+            const float ey = interp(a.Eyf, i00, i10, i01, i11, rx, ry);
+            const float qf = a.q[p] * maxq;
+            const float coef = a.m ? __fdiv_rn(-qf, a.m[p]) : -qf;
+            vxx = vxx + (coef * ex) * a.dtf;
+            vyy = vyy + (coef * ey) * a.dtf;
+            a.vx[p] = vxx;
+            a.vy[p] = vyy;
+        }
+        if constexpr (PUSH) {
+            drift(rx, ix, vxx, a.dtdx, a.Nx);
+            drift(ry, iy, vyy, a.dtdy, a.Ny);
+            a.xr[p] = rx;
+            a.yr[p] = ry;
+            a.cell[p] = (uint32_t)iy * (uint32_t)a.Nx + (uint32_t)ix;
+        }
+    }
+}
+
+int move(pic_ctx* c, double dt, bool gather, bool push) {
+    if (c->n == 0) return PIC_OK;
+    if (gather) PIC_TRY(ensure_fields(c));
+    MoveArgs a;
+    a.cell = c->cell;
+    a.xr = c->xr;
+    a.yr = c->yr;
+    a.vx = c->vx;
+    a.vy = c->vy;
+    a.q = c->q;
+    a.m = c->has_mass ? c->m : nullptr;
+    a.Exf = c->Exf;
+    a.Eyf = c->Eyf;
+    a.n = c->n;
+    a.Nx = c->Nx;
+    a.Ny = c->Ny;
+    a.dtf = (float)dt;
+    a.dtdx = (float)(dt / c->dx);
+    a.dtdy = (float)(dt / c->dy);
+    a.st = c->dstats;
+    int sms = 148;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    size_t blocks = (c->n + 255) / 256;
+    if (blocks > (size_t)sms * 32) blocks = (size_t)sms * 32;
+    prof_begin(c, gather && push ? "gather_push" : gather ? "gather" : "push");
+    if (gather && push)
+        move_particles<true, true><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    else if (gather)
+        move_particles<true, false><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    else
+        move_particles<false, true><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    prof_end(c);
+    PIC_TRY(check_launch(c, "move_particles"));
+    if (push) c->sorted = 0;
+    return PIC_OK;
+}
+
+}  // namespace picgb
+
+using namespace picgb;
+
+extern "C" {
+
+int pic_gpu_gather(pic_ctx* c, double dt) {
+    if (!c) return fail(PIC_ERR_ARG, "NULL context");
+    PIC_CUDA_TRY(cudaSetDevice(c->device));
+    return move(c, dt, true, false);
+}
+
+int pic_gpu_push(pic_ctx* c, double dt) {
+    if (!c) return fail(PIC_ERR_ARG, "NULL context");
+    PIC_CUDA_TRY(cudaSetDevice(c->device));
+    return move(c, dt, false, true);
+}
+
+int pic_gpu_gather_push(pic_ctx* c, double dt) {
+    if (!c) return fail(PIC_ERR_ARG, "NULL context");
+    PIC_CUDA_TRY(cudaSetDevice(c->device));
+    return move(c, dt, true, true);
+}
+
+}  // extern "C"

@@ -76,6 +76,14 @@ _SIGS = [
     ("pic_gpu_profile_read", [_vp, C.c_char_p, _dp, C.POINTER(C.c_longlong)]),
     ("pic_gpu_host_alloc", [C.c_size_t, C.POINTER(_vp)]),
     ("pic_gpu_host_free", [_vp]),
+    ("pic_gpu_set_rho", [_vp, _vp]),
+    ("pic_gpu_set_fields", [_vp, _vp, _vp, _vp]),
+    ("pic_gpu_get_fields", [_vp, _vp, _vp, _vp]),
+    ("pic_gpu_poisson_fft", [_vp]),
+    ("pic_gpu_gather", [_vp, C.c_double]),
+    ("pic_gpu_push", [_vp, C.c_double]),
+    ("pic_gpu_gather_push", [_vp, C.c_double]),
+    ("pic_gpu_diagnostics", [_vp, C.POINTER(_Diag)]),
 ]
 
 
@@ -236,6 +244,37 @@ class Context:
         cnt = C.c_longlong()
         _check(lib().pic_gpu_profile_read(self.h, kernel.encode(), C.byref(ms), C.byref(cnt)))
         return ms.value, cnt.value
+
+    # ---- fields / Poisson / motion / diagnostics ----
+    def set_rho(self, rho):
+        r = _arr(rho, np.float64)
+        _check(lib().pic_gpu_set_rho(self.h, _ptr(r)))
+
+    def set_fields(self, phi=None, ex=None, ey=None):
+        a = [_arr(v, np.float64) for v in (phi, ex, ey)]
+        _check(lib().pic_gpu_set_fields(self.h, *[_ptr(v) for v in a]))
+
+    def fields(self):
+        out = [np.zeros(self.G) for _ in range(3)]
+        _check(lib().pic_gpu_get_fields(self.h, *[_ptr(v) for v in out]))
+        return tuple(out)
+
+    def poisson_fft(self):
+        _check(lib().pic_gpu_poisson_fft(self.h))
+
+    def gather(self, dt):
+        _check(lib().pic_gpu_gather(self.h, float(dt)))
+
+    def push(self, dt):
+        _check(lib().pic_gpu_push(self.h, float(dt)))
+
+    def gather_push(self, dt):
+        _check(lib().pic_gpu_gather_push(self.h, float(dt)))
+
+    def diagnostics(self) -> dict:
+        d = _Diag()
+        _check(lib().pic_gpu_diagnostics(self.h, C.byref(d)))
+        return {k: getattr(d, k) for k, _ in _Diag._fields_}
 
     def synchronize(self):
         _check(lib().pic_gpu_synchronize(self.h))
