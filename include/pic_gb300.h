@@ -60,9 +60,10 @@ extern "C" {
 #define PIC_SCHEME_ESIRKEPOV 3 /* the reference's trajectory-averaged rho (ngp.cpp:13-84) */
 
 /* ---- deposit ordering modes ---- */
-#define PIC_ORDER_AUTO 0     /* tiled shared-memory kernel when cell-sorted, else atomic kernel */
-#define PIC_ORDER_SORTED 1   /* require cell-sorted particles (PIC_ERR_STATE otherwise)        */
-#define PIC_ORDER_UNSORTED 2 /* global-atomic kernel regardless of order                        */
+#define PIC_ORDER_AUTO 0     /* tiled kernel when cell-sorted, else the run-aggregating kernel   */
+#define PIC_ORDER_SORTED 1   /* tiled kernel; PIC_ERR_STATE unless cell-sorted                   */
+#define PIC_ORDER_UNSORTED 2 /* run-aggregating kernel (any order; fast when nearly sorted)      */
+#define PIC_ORDER_ATOMIC 3   /* one thread per particle, one int64 atomic per stencil node       */
 
 /* Mirrors pic::Domain (src/pic/domain.hpp:7-44): periodic box [0,Lx)x[0,Ly),
  * Nx x Ny cells, dx = Lx/Nx, dy = Ly/Ny. */

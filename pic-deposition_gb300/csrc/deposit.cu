@@ -13,20 +13,24 @@
 //    summation order: the tiled, atomic and oracle paths agree bit for bit.
 //    |value| <= 2^24 (+ a few units of remainder), so a warp-wide partial sum
 //    fits in int32.
+//  * Warp step (both fast paths). A warp handles 128 consecutive particles at
+//    a time: lane l takes particles 4l..4l+3, loaded with one 128-bit streaming
+//    load per field (each warp load is 512 contiguous bytes; the next step's
+//    loads are issued before this step's arithmetic). A lane sums its
+//    particles' stencil values in registers while they share a cell, then a
+//    segmented warp scan over the lanes' (cell, sums) leaves each run of equal
+//    cells' total in the run's last lane, which issues the atomics.
 //  * Sorted path (deposit_tiled). One CTA per tile of tile_w x tile_h cells;
 //    its int64 accumulators (tile + halo of 1 cell below, 2 above) live in
 //    shared memory. Warp w walks rows w, w+8, ... of the tile; the particles of
 //    one row of the tile are one contiguous run of the cell-sorted stream,
-//    [offsets[c0], offsets[c0+tile_w]). Each warp step loads 32 particles
-//    coalesced (streaming loads, the particle stream is read once), computes
-//    every lane's stencil frame, and combines lanes of the same cell before any
-//    atomic: with one or two cells in the step, a transposed warp reduction
-//    leaves each frame node's warp total in one lane (V values in about V
-//    shuffles), and those lanes issue one shared atomic each. Steps with three
-//    or more cells fall back to per-lane shared atomics. At the end the tile
-//    is flushed to the global int64 grid with one atomic per non-zero node.
-//  * Unsorted path (deposit_atomic): one thread per particle, int64 atomics
-//    straight into the L2-resident global grid.
+//    [offsets[c0], offsets[c0+tile_w]). Run totals go to shared memory; at the
+//    end the tile is flushed to the global int64 grid once.
+//  * Any-order path (deposit_runs): the same warp step over the whole array,
+//    run totals straight to the global int64 grid (L2-resident). Needs no
+//    offsets; fast when particles are nearly cell-ordered (between sorts).
+//  * Naive path (deposit_atomic): one thread per particle, one int64 atomic
+//    per stencil node into the global grid.
 //
 // Stencil frames (weights relative to the particle's own cell, identical to the
 // oracle's restatement):
@@ -458,6 +462,95 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_tiled(DepArgs a) {
     }
 }
 
+// Adds a lane's sums for cell `key` straight to the global grid.
+template <int S>
+__device__ __forceinline__ void flush_global(const DepArgs& a, uint32_t key, const int (&acc)[Frame<S>::NX * Frame<S>::NX]) {
+    constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO;
+    const int iy = (int)(key / (uint32_t)a.Nx), ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
+#pragma unroll
+    for (int j = 0; j < NX; ++j) {
+        const size_t row = (size_t)wrap_i(iy + LO + j, a.Ny) * a.Nx;
+#pragma unroll
+        for (int i = 0; i < NX; ++i) {
+            const int v = acc[j * NX + i];
+            if (v != 0) atomicAdd(a.acc + row + wrap_i(ix + LO + i, a.Nx), (unsigned long long)(long long)v);
+        }
+    }
+}
+
+// Any-order path with run aggregation: the sorted path's warp step (4
+// consecutive particles per lane, register sums per cell, segmented warp scan)
+// over the whole particle array, with the run totals added straight to the
+// global int64 grid. It needs no per-cell offsets and is correct for any order;
+// runs are long when the particles are nearly cell-ordered, as between the
+// sorts of a time-stepping loop.
+template <int S>
+__global__ void __launch_bounds__(DEP_THREADS) deposit_runs(DepArgs a) {
+    constexpr int NX = Frame<S>::NX, V = Frame<S>::V;
+    constexpr int NV = NX * NX;
+    const int lane = threadIdx.x & 31;
+    const size_t gw = (size_t)blockIdx.x * DEP_WARPS + (threadIdx.x >> 5);
+    const size_t stride = (size_t)gridDim.x * DEP_WARPS * 128;
+    const uint32_t G = (uint32_t)a.Nx * (uint32_t)a.Ny;
+    const unsigned upto = (lane == 31) ? FULL : ((2u << lane) - 1u);
+    size_t base = gw * 128;
+    Quad<S> cur, nxt;
+    load_quad<S>(a, (uint32_t)(base + 4u * lane), base + 4u * lane < a.n, cur);
+    for (; base < a.n; base += stride) {
+        const size_t nbase = base + stride;
+        if (nbase < a.n) load_quad<S>(a, (uint32_t)(nbase + 4u * lane), nbase + 4u * lane < a.n, nxt);
+        uint32_t ckey = NO_CELL;
+        int acc[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) acc[q] = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const size_t p = base + 4u * lane + (size_t)k;
+            if (p < a.n) {
+                const uint32_t key = u4(cur.cell, k);
+                if (key >= G) {
+                    set_dev_error(a.st, DEV_BAD_CELL, (unsigned)p);
+                    continue;
+                }
+                const int iy = (int)(key / (uint32_t)a.Nx);
+                int val[V];
+                float vxx = 0.0f, vyy = 0.0f;
+                if constexpr (S == S_ESK) {
+                    vxx = f4(cur.vx, k);
+                    vyy = f4(cur.vy, k);
+                }
+                if (!stencil_values<S>(a, f4(cur.xr, k), f4(cur.yr, k), f4(cur.q, k), vxx, vyy,
+                                       (int)(key - (uint32_t)iy * (uint32_t)a.Nx), iy, p, val))
+                    continue;
+                if (key != ckey) {
+                    if (ckey != NO_CELL) flush_global<S>(a, ckey, acc);
+                    ckey = key;
+#pragma unroll
+                    for (int q = 0; q < NV; ++q) acc[q] = val[q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < NV; ++q) acc[q] += val[q];
+                }
+            }
+        }
+        const uint32_t kprev = __shfl_up_sync(FULL, ckey, 1);
+        const unsigned H = __ballot_sync(FULL, lane == 0 || ckey != kprev);
+        const int segstart = 31 - __clz(H & upto);
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const bool take = lane - d >= segstart;
+#pragma unroll
+            for (int q = 0; q < NV; ++q) {
+                const int o = __shfl_up_sync(FULL, acc[q], d);
+                if (take) acc[q] += o;
+            }
+        }
+        const bool tail = (lane == 31) || ((H >> (lane + 1)) & 1u);
+        if (tail && ckey != NO_CELL) flush_global<S>(a, ckey, acc);
+        cur = nxt;
+    }
+}
+
 template <int S>
 __global__ void __launch_bounds__(DEP_THREADS) deposit_atomic(DepArgs a) {
     constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
@@ -497,8 +590,9 @@ __global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double
 }
 
 template <int S>
-static int launch_deposit(pic_ctx* c, const DepArgs& a, bool tiled) {
-    if (tiled) {
+// kernel choice: 0 tiled (cell-sorted), 1 run-aggregating (any order), 2 one thread per particle
+static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
+    if (kind == 0) {
         const size_t smem = (size_t)(a.tile_h + 3) * (a.tile_w + 3) * sizeof(long long);
         const unsigned tiles = (unsigned)(a.tiles_x * ((c->Ny + a.tile_h - 1) / a.tile_h));
         prof_begin(c, "deposit");
@@ -508,6 +602,16 @@ static int launch_deposit(pic_ctx* c, const DepArgs& a, bool tiled) {
     }
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (kind == 1) {
+        size_t blocks = (a.n + DEP_THREADS * 4 - 1) / (DEP_THREADS * 4);
+        const size_t cap = (size_t)sms * 8;
+        if (blocks > cap) blocks = cap;
+        if (blocks == 0) blocks = 1;
+        prof_begin(c, "deposit");
+        deposit_runs<S><<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
+        prof_end(c);
+        return check_launch(c, "deposit_runs");
+    }
     size_t blocks = (a.n + DEP_THREADS - 1) / DEP_THREADS;
     const size_t cap = (size_t)sms * 16;
     if (blocks > cap) blocks = cap;
@@ -520,14 +624,16 @@ static int launch_deposit(pic_ctx* c, const DepArgs& a, bool tiled) {
 
 int deposit_rho(pic_ctx* c, int scheme, double dt, double background) {
     if (scheme < PIC_SCHEME_NGP || scheme > PIC_SCHEME_ESIRKEPOV) return fail(PIC_ERR_ARG, "unknown scheme");
-    bool tiled;
+    int tiled;  // kernel kind, see launch_deposit
     if (c->order_mode == PIC_ORDER_SORTED) {
         if (!c->sorted) return fail(PIC_ERR_STATE, "deposit: PIC_ORDER_SORTED needs cell-sorted particles");
-        tiled = true;
+        tiled = 0;
     } else if (c->order_mode == PIC_ORDER_UNSORTED) {
-        tiled = false;
+        tiled = 1;
+    } else if (c->order_mode == PIC_ORDER_ATOMIC) {
+        tiled = 2;
     } else {
-        tiled = c->sorted != 0;
+        tiled = c->sorted ? 0 : 1;
     }
     PIC_CUDA_TRY(cudaMemsetAsync(c->acc, 0, c->G * sizeof(long long), c->stream));
     DepArgs a;
@@ -583,7 +689,7 @@ extern "C" {
 
 int pic_gpu_set_deposit_order(pic_ctx* c, int order) {
     if (!c) return fail(PIC_ERR_ARG, "NULL context");
-    if (order < PIC_ORDER_AUTO || order > PIC_ORDER_UNSORTED) return fail(PIC_ERR_ARG, "unknown order mode");
+    if (order < PIC_ORDER_AUTO || order > PIC_ORDER_ATOMIC) return fail(PIC_ERR_ARG, "unknown order mode");
     c->order_mode = order;
     return PIC_OK;
 }

@@ -32,7 +32,7 @@ ERRORS = {
     -1: "PIC_ERR_ARG", -2: "PIC_ERR_CUDA", -3: "PIC_ERR_NOMEM", -4: "PIC_ERR_STATE", -5: "PIC_ERR_OVERFLOW",
     -6: "PIC_ERR_COURANT", -7: "PIC_ERR_TIMEOUT", -8: "PIC_ERR_UNSUPPORTED", -9: "PIC_ERR_DEVICE",
 }
-ORDER_AUTO, ORDER_SORTED, ORDER_UNSORTED = 0, 1, 2
+ORDER_AUTO, ORDER_SORTED, ORDER_UNSORTED, ORDER_ATOMIC = 0, 1, 2, 3
 
 
 class PicError(RuntimeError):

@@ -23,6 +23,8 @@ def gpu_deposit(pg, nx, ny, lx, ly, p, scheme, dt=0.0, order="sorted", tile=None
         c.upload(p["x"], p["y"], p["q"], p.get("vx"), p.get("vy"), p.get("m"))
         if order == "sorted":
             c.sort()
+        elif order == "atomic":
+            c.set_order(pg.ORDER_ATOMIC)
         else:
             c.set_order(pg.ORDER_UNSORTED)
         if tile:
@@ -96,7 +98,7 @@ def test_gpu_deposit_128(port, pg):
 
 # ---- shapes, tiles and orders -------------------------------------------
 @pytest.mark.parametrize("scheme", [NGP, CIC, TSC, ESK])
-@pytest.mark.parametrize("order", ["sorted", "unsorted"])
+@pytest.mark.parametrize("order", ["sorted", "unsorted", "atomic"])
 @pytest.mark.parametrize("grid", [(37, 23, 3.7, 2.3), (64, 64, 64.0, 64.0), (1, 1, 1.0, 1.0), (2, 3, 2.0, 3.0),
                                   (200, 5, 20.0, 0.5)])
 def test_grids(port, pg, scheme, order, grid):
@@ -118,7 +120,29 @@ def test_sorted_equals_unsorted_bitwise(port, pg, scheme):
     _, a, ua, _ = gpu_deposit(pg, 50, 70, 5.0, 7.0, p, scheme, 0.02, "sorted")
     _, b, ub, _ = gpu_deposit(pg, 50, 70, 5.0, 7.0, p, scheme, 0.02, "unsorted")
     _, c, _, _ = gpu_deposit(pg, 50, 70, 5.0, 7.0, p, scheme, 0.02, "sorted", (5, 9))
-    assert ua == ub and np.array_equal(a, b) and np.array_equal(a, c)
+    _, d, _, _ = gpu_deposit(pg, 50, 70, 5.0, 7.0, p, scheme, 0.02, "atomic")
+    assert ua == ub and np.array_equal(a, b) and np.array_equal(a, c) and np.array_equal(a, d)
+
+
+@pytest.mark.parametrize("scheme", [NGP, CIC, TSC, ESK])
+def test_nearly_sorted_after_push(port, pg, scheme):
+    # sort, then push: particles are nearly cell-ordered; AUTO uses the run-aggregating kernel
+    p = maxwellian(port, 64, 48, 6.4, 4.8, 200000, seed=12, T=0.05)
+    with pg.Context(64, 48, 6.4, 4.8, len(p["x"])) as c:
+        c.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+        c.sort()
+        c.push(0.3)
+        assert not c.is_sorted()
+        c.deposit(scheme, 0.05, download=False)
+        acc, unit = c.rho_fixed()
+        lay = c.device_layout()
+        c.set_order(pg.ORDER_ATOMIC)
+        c.deposit(scheme, 0.05, download=False)
+        acc2, _ = c.rho_fixed()
+    _, maxq = port.normalize_charge(p["q"])
+    want, wunit = port.deposit_fixed(64, 48, 6.4, 4.8, scheme, lay["cell"], lay["xr"], lay["yr"], lay["q"], maxq,
+                                     lay["vx"], lay["vy"], 0.05)
+    assert unit == wunit and np.array_equal(acc, want) and np.array_equal(acc2, want)
 
 
 # ---- edge cases ------------------------------------------------------------
