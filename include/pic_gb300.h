@@ -163,6 +163,16 @@ int pic_gpu_get_fields(pic_ctx* ctx, double* phi, double* Ex, double* Ey);
  * E = -(phi[i+1]-phi[i])/dx. FP64 cuFFT (D2Z/Z2D) plus this library's kernels. */
 int pic_gpu_poisson_fft(pic_ctx* ctx);
 
+/* ---- Poisson by red-black Gauss-Seidel (new; the reference's PoissonSolverGS,
+ *      src/pic/poisson_gs.cpp:11-61, is lexicographic with a max|dphi| stop) ----
+ * Same 5-point stencil and sign; right-hand side rho*dV minus its mean; starts
+ * from the context's phi when warm_start != 0 (the previous solve's, or one set
+ * with pic_gpu_set_fields), else from 0; stops when ||b - A phi||_2/||b||_2 <= tol
+ * (checked every check_every sweeps) or after max_iters sweeps; removes the mean
+ * of phi and computes E. FP64. Needs even Nx and Ny (PIC_ERR_UNSUPPORTED). */
+int pic_gpu_poisson_rbgs(pic_ctx* ctx, double tol, int max_iters, int warm_start, int check_every, int* iters_out,
+                         double* resid_out);
+
 /* ---- particle motion ---- */
 
 /* pic::gatherFieldsSoA (src/deposition/deposition.cpp:335-356): v += -(q/m)*E*dt. */
@@ -175,6 +185,24 @@ int pic_gpu_gather_push(pic_ctx* ctx, double dt);
 /* ---- diagnostics: pic::computeDiagnostics (src/pic/diagnostics.cpp:42-51), FP64 sums
  *      in a fixed order (bit-identical run to run) ---- */
 int pic_gpu_diagnostics(pic_ctx* ctx, pic_diag* out);
+
+/* ---- time stepping: replaces pic::Simulation::run's loop (src/pic/simulation.cpp:69-145) ----
+ * NGP/CIC/TSC: push -> [sort] -> deposit -> +background -> Poisson -> gather -> diagnostics;
+ * Esirkepov rho: deposit -> +background -> Poisson -> push -> gather -> diagnostics. */
+typedef struct pic_run_config {
+    int scheme;            /* PIC_SCHEME_* of the charge deposit */
+    int poisson;           /* 0: FFT (PoissonSolverFFT), 1: red-black Gauss-Seidel warm-started from phi */
+    double dt;             /* Domain::dt; also the Esirkepov path length v*dt */
+    double background;     /* added to rho after each deposit (applyBackgroundIfNeeded, simulation.cpp:52-59) */
+    int sort_interval;     /* in-place cell sort every k steps (0: never); results do not depend on it */
+    int use_graph;         /* replay the step as a CUDA graph (FFT Poisson only) */
+    double rbgs_tol;       /* poisson == 1: relative residual target */
+    int rbgs_max_iters;    /* poisson == 1: sweep limit per solve */
+    int rbgs_check_every;  /* poisson == 1: sweeps between residual checks */
+} pic_run_config;
+/* Advances `steps` steps; history (steps entries, may be NULL) receives every
+ * step's diagnostics (SimulationResult::*_history, simulation.hpp:49-60). */
+int pic_gpu_run(pic_ctx* ctx, const pic_run_config* cfg, int steps, pic_diag* history);
 
 /* ---- deposit for callers that cannot allocate device memory ----
  *

@@ -383,6 +383,52 @@ def spectral_noise(nx: int, ny: int, rho: np.ndarray) -> float:
     return float(power[high].sum() / total)
 
 
+def simulate(port: "Port", nx, ny, lx, ly, p, scheme, dt, steps, background=0.0, record_field_from=0):
+    """pic::Simulation::run's loop (src/pic/simulation.cpp:82-131) in FP64 over
+    the port, with the FFT Poisson solve: NGP/CIC/TSC push -> deposit ->
+    background -> solve -> gather; Esirkepov deposit -> background -> solve ->
+    push -> gather. Returns (history (steps, 6) in pic_diag order, particles)."""
+    p = {k: np.array(v, dtype=np.float64, copy=True) for k, v in p.items()}
+    n = len(p["x"])
+    p.setdefault("m", np.ones(n))
+    hist = np.zeros((steps, 6))
+    vol = (lx / nx) * (ly / ny)
+    qsum, qabs = p["q"].sum(), np.abs(p["q"]).sum()
+    for s in range(steps):
+        if scheme != ESIRKEPOV:
+            p["x"], p["y"] = port.push_ref(nx, ny, lx, ly, p, dt)
+        rho = port.deposit_ref(nx, ny, lx, ly, scheme, p, dt=dt) + background
+        phi, ex, ey = poisson_fft(nx, ny, lx, ly, rho)
+        if scheme == ESIRKEPOV:
+            p["x"], p["y"] = port.push_ref(nx, ny, lx, ly, p, dt)
+        p["vx"], p["vy"] = port.gather_ref(nx, ny, lx, ly, p, ex, ey, dt)
+        ke = float(np.sum(0.5 * p["m"] * (p["vx"] ** 2 + p["vy"] ** 2)))
+        fe = 0.5 * float(np.sum(ex * ex + ey * ey)) * vol
+        ir = float(rho.sum()) * vol
+        hist[s] = (abs(ir - qsum) / max(qabs, 1e-12), qsum, ir, ke, fe, ke + fe)
+    return hist, p
+
+
+def dominant_frequency(signal, dt):
+    """estimateDominantFrequency, src/pic/validation.cpp:19-54: the k = 1..n/2-1
+    DFT bin of largest power of the mean-removed signal, returned as k/(n*dt)."""
+    x = np.asarray(signal, dtype=np.float64)
+    n = len(x)
+    if n < 8:
+        return 0.0
+    c = x - x.mean()
+    t = np.arange(n)
+    best_p, best_k = 0.0, 1
+    for k in range(1, n // 2):
+        ph = 2.0 * np.pi * (k * t) / n
+        re = np.sum(c * np.cos(ph))
+        im = -np.sum(c * np.sin(ph))
+        pw = re * re + im * im
+        if pw > best_p:
+            best_p, best_k = pw, k
+    return best_k / (n * dt)
+
+
 def poisson_fft(nx: int, ny: int, lx: float, ly: float, rho: np.ndarray):
     """PoissonSolverFFT::solve, src/pic/poisson_fft.cpp:45-94: phi_hat =
     (rho*dV)_hat / k^2 with continuous k = 2*pi*m/L, DC set to 0, then the

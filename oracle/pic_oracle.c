@@ -506,14 +506,16 @@ double orc_rbgs_residual(const orc_domain* d, const double* b, const double* phi
     const double dx = dom_dx(d), dy = dom_dy(d);
     const double dx2 = dx * dx, dy2 = dy * dy;
     const double denom = 2.0 * (1.0 / dx2 + 1.0 / dy2);
+    const double ix2 = 1.0 / dx2, iy2 = 1.0 / dy2;
     double rr = 0.0, bb = 0.0;
     for (int j = 0; j < ny; ++j)
         for (int i = 0; i < nx; ++i) {
             const int im = (i - 1 + nx) % nx, ip = (i + 1) % nx;
             const int jm = (j - 1 + ny) % ny, jp = (j + 1) % ny;
             const size_t id = (size_t)j * nx + i;
-            const double ap = denom * phi[id] - (phi[(size_t)j * nx + im] + phi[(size_t)j * nx + ip]) / dx2 -
-                              (phi[(size_t)jm * nx + i] + phi[(size_t)jp * nx + i]) / dy2;
+            const double we = phi[(size_t)j * nx + im] + phi[(size_t)j * nx + ip];
+            const double sn = phi[(size_t)jm * nx + i] + phi[(size_t)jp * nx + i];
+            const double ap = (denom * phi[id] - we * ix2) - sn * iy2;
             const double r = b[id] - ap;
             rr += r * r;
             bb += b[id] * b[id];
@@ -527,21 +529,24 @@ int orc_rbgs(const orc_domain* d, const double* rho, double* phi, double tol, in
     if ((nx & 1) || (ny & 1)) return -1;
     const double dx = dom_dx(d), dy = dom_dy(d);
     const double dx2 = dx * dx, dy2 = dy * dy;
+    const double ix2 = 1.0 / dx2, iy2 = 1.0 / dy2;
     const double denom = 2.0 * (1.0 / dx2 + 1.0 / dy2);
+    const double inv_denom = 1.0 / denom;
     double* b = rbgs_rhs(d, rho);
     if (check_every < 1) check_every = 1;
     double res = orc_rbgs_residual(d, b, phi);
     int it = 0;
     while (it < max_iters && !(res <= tol)) {
+        /* multiplications by 1/dx^2, 1/dy^2, 1/denom, in the GPU kernel's order */
         for (int color = 0; color < 2; ++color)
             for (int j = 0; j < ny; ++j)
                 for (int i = (j + color) & 1; i < nx; i += 2) {
                     const int im = (i - 1 + nx) % nx, ip = (i + 1) % nx;
                     const int jm = (j - 1 + ny) % ny, jp = (j + 1) % ny;
                     const size_t id = (size_t)j * nx + i;
-                    phi[id] = ((phi[(size_t)j * nx + im] + phi[(size_t)j * nx + ip]) / dx2 +
-                               (phi[(size_t)jm * nx + i] + phi[(size_t)jp * nx + i]) / dy2 + b[id]) /
-                              denom;
+                    const double we = phi[(size_t)j * nx + im] + phi[(size_t)j * nx + ip];
+                    const double sn = phi[(size_t)jm * nx + i] + phi[(size_t)jp * nx + i];
+                    phi[id] = ((we * ix2 + sn * iy2) + b[id]) * inv_denom;
                 }
         ++it;
         if (it % check_every == 0 || it == max_iters) res = orc_rbgs_residual(d, b, phi);

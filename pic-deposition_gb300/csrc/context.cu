@@ -365,6 +365,7 @@ int pic_gpu_destroy(pic_ctx* c) {
                     c->cellcount, c->scan.partials, c->stage, c->acc, c->rho, c->unitbuf, c->dstats};
     for (void* p : ptrs) dfree(p);
     release_fields(c);
+    release_rbgs(c);
     prof_clear(c, nullptr);
     delete c->prof;
     if (c->stream) cudaStreamDestroy(c->stream);

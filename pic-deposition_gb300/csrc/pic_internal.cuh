@@ -92,6 +92,12 @@ struct pic_ctx {
     // deterministic FP64 reductions
     double* red_partials = nullptr;
     double* red_out = nullptr;
+    // red-black Gauss-Seidel
+    double *rb_b = nullptr, *rb_partial = nullptr, *rb_scalars = nullptr;
+    int last_rbgs_iters = 0;
+    double last_rbgs_resid = 0.0;
+    // kernels inside the captured time-step graphs (for the launch counter)
+    long long graph_launches_sort = 0, graph_launches_plain = 0;
 
     picgb::DevStats* dstats = nullptr;
 
@@ -140,6 +146,7 @@ int efield_from_phi(pic_ctx* ctx);
 int diagnostics_async(pic_ctx* ctx);
 int read_diagnostics(pic_ctx* ctx, pic_diag* d);
 void release_fields(pic_ctx* ctx);
+void release_rbgs(pic_ctx* ctx);
 // Deposit (deposit.cu).
 int deposit_rho(pic_ctx* ctx, int scheme, double dt, double background);
 

@@ -1,0 +1,240 @@
+// Red-black Gauss-Seidel Poisson solve (FP64).
+//
+// PoissonSolverGS::solve (src/pic/poisson_gs.cpp:11-61) is lexicographic,
+// zeroes phi on every call and stops on max|dphi| < 1e-6. This solver keeps its
+// 5-point stencil and sign, phi = ((phiW+phiE)/dx^2 + (phiS+phiN)/dy^2 + rho*dV)
+// / (2(1/dx^2+1/dy^2)) (poisson_gs.cpp:32-38), and changes what the benchmark spec
+// asks for: red-black ordering (all points with (i+j) even, then odd; each
+// colour is one data-parallel kernel), the right-hand side rho*dV with its mean
+// removed (the periodic problem is singular), a warm start from the phi already
+// in the context (the previous step's, or a learned guess), and the stop
+// ||b - A phi||_2 / ||b||_2 <= tol checked every `check_every` sweeps. On exit
+// phi has its mean removed and E is the forward difference of phi
+// (poisson_gs.cpp:48-60). Multiplications by 1/dx^2, 1/dy^2 and 1/denom
+// replace the reference's divisions (FP64 division is slow on this part); the
+// oracle's restatement uses the same order of operations.
+//
+// Sums (mean, residual norms) use a fixed two-level tree, so results are
+// identical run to run. Odd Nx or Ny is rejected: the colouring would not be a
+// valid red-black split across the periodic seam.
+#include "pic_internal.cuh"
+
+namespace picgb {
+
+constexpr int RB_THREADS = 256;
+constexpr int RB_RED_BLOCKS = 1024;
+
+struct RbArgs {
+    double* phi;
+    const double* b;
+    int Nx, Ny;
+    double ix2, iy2, inv_denom, denom;
+};
+
+__global__ void rbgs_half(RbArgs a, int color) {
+    const int hx = a.Nx >> 1;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)hx * a.Ny) return;
+    const int j = (int)(t / hx);
+    const int i = 2 * (int)(t - (size_t)j * hx) + ((j + color) & 1);
+    const int im = i == 0 ? a.Nx - 1 : i - 1, ip = i == a.Nx - 1 ? 0 : i + 1;
+    const int jm = j == 0 ? a.Ny - 1 : j - 1, jp = j == a.Ny - 1 ? 0 : j + 1;
+    const size_t id = (size_t)j * a.Nx + i;
+    const double we = __dadd_rn(a.phi[(size_t)j * a.Nx + im], a.phi[(size_t)j * a.Nx + ip]);
+    const double sn = __dadd_rn(a.phi[(size_t)jm * a.Nx + i], a.phi[(size_t)jp * a.Nx + i]);
+    a.phi[id] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(we, a.ix2), __dmul_rn(sn, a.iy2)), a.b[id]), a.inv_denom);
+}
+
+__device__ __forceinline__ double rb_block_sum(double v) {
+    __shared__ double ws[RB_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) ws[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < RB_THREADS / 32; ++w) s = __dadd_rn(s, ws[w]);
+    __syncthreads();
+    return s;
+}
+
+// partial[blk] = sum of rho*vol over a fixed chunk
+__global__ void rb_sum_rhs(const double* __restrict__ rho, double vol, size_t g, double* __restrict__ partial) {
+    const size_t chunk = (g + RB_RED_BLOCKS - 1) / RB_RED_BLOCKS;
+    const size_t b = (size_t)blockIdx.x * chunk, e = b + chunk < g ? b + chunk : g;
+    double s = 0.0;
+    for (size_t i = b + threadIdx.x; i < e; i += RB_THREADS) s = __dadd_rn(s, __dmul_rn(rho[i], vol));
+    const double t = rb_block_sum(s);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+// partial[2*blk] = sum r^2, partial[2*blk+1] = sum b^2 with r = b - A phi
+__global__ void rb_resid_partials(RbArgs a, double* __restrict__ partial) {
+    const size_t g = (size_t)a.Nx * a.Ny;
+    const size_t chunk = (g + RB_RED_BLOCKS - 1) / RB_RED_BLOCKS;
+    const size_t b0 = (size_t)blockIdx.x * chunk, e = b0 + chunk < g ? b0 + chunk : g;
+    double rr = 0.0, bb = 0.0;
+    for (size_t id = b0 + threadIdx.x; id < e; id += RB_THREADS) {
+        const int j = (int)(id / a.Nx), i = (int)(id - (size_t)j * a.Nx);
+        const int im = i == 0 ? a.Nx - 1 : i - 1, ip = i == a.Nx - 1 ? 0 : i + 1;
+        const int jm = j == 0 ? a.Ny - 1 : j - 1, jp = j == a.Ny - 1 ? 0 : j + 1;
+        const double we = __dadd_rn(a.phi[(size_t)j * a.Nx + im], a.phi[(size_t)j * a.Nx + ip]);
+        const double sn = __dadd_rn(a.phi[(size_t)jm * a.Nx + i], a.phi[(size_t)jp * a.Nx + i]);
+        const double ap = __dsub_rn(__dsub_rn(__dmul_rn(a.denom, a.phi[id]), __dmul_rn(we, a.ix2)), __dmul_rn(sn, a.iy2));
+        const double r = __dsub_rn(a.b[id], ap);
+        rr = __dadd_rn(rr, __dmul_rn(r, r));
+        bb = __dadd_rn(bb, __dmul_rn(a.b[id], a.b[id]));
+    }
+    const double t1 = rb_block_sum(rr);
+    const double t2 = rb_block_sum(bb);
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = t1;
+        partial[2 * blockIdx.x + 1] = t2;
+    }
+}
+
+// out[0] = sum of partial[0..n) (stride `stride`, offset `off`)
+__global__ void rb_final(const double* __restrict__ partial, int n, int stride, int off, double* out) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += RB_THREADS) s = __dadd_rn(s, partial[(size_t)i * stride + off]);
+    const double t = rb_block_sum(s);
+    if (threadIdx.x == 0) *out = t;
+}
+
+// b = rho*vol - mean, mean = sum / g
+__global__ void rb_make_rhs(const double* __restrict__ rho, double vol, size_t g, const double* __restrict__ sum,
+                            double* __restrict__ b) {
+    const double mean = __ddiv_rn(*sum, (double)g);
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < g) b[i] = __dsub_rn(__dmul_rn(rho[i], vol), mean);
+}
+
+__global__ void rb_sub_mean(double* __restrict__ phi, size_t g, const double* __restrict__ sum) {
+    const double mean = __ddiv_rn(*sum, (double)g);
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < g) phi[i] = __dsub_rn(phi[i], mean);
+}
+
+static int ensure_rbgs(pic_ctx* c) {
+    PIC_TRY(ensure_fields(c));
+    int rc = PIC_OK;
+    if (!c->rb_b) c->rb_b = (double*)dalloc(c->G * 8, &rc);
+    if (rc) return rc;
+    if (!c->rb_partial) c->rb_partial = (double*)dalloc(2 * RB_RED_BLOCKS * 8, &rc);
+    if (rc) return rc;
+    if (!c->rb_scalars) c->rb_scalars = (double*)dalloc(8 * 8, &rc);
+    return rc;
+}
+
+static RbArgs rb_args(pic_ctx* c) {
+    RbArgs a;
+    a.phi = c->phi;
+    a.b = c->rb_b;
+    a.Nx = c->Nx;
+    a.Ny = c->Ny;
+    const double dx2 = c->dx * c->dx, dy2 = c->dy * c->dy;
+    a.ix2 = 1.0 / dx2;
+    a.iy2 = 1.0 / dy2;
+    a.denom = 2.0 * (1.0 / dx2 + 1.0 / dy2);
+    a.inv_denom = 1.0 / a.denom;
+    return a;
+}
+
+static int rb_sweeps(pic_ctx* c, const RbArgs& a, int n) {
+    const size_t half = (size_t)(c->Nx / 2) * c->Ny;
+    const unsigned blocks = (unsigned)((half + RB_THREADS - 1) / RB_THREADS);
+    for (int s = 0; s < n; ++s) {
+        rbgs_half<<<blocks, RB_THREADS, 0, c->stream>>>(a, 0);
+        PIC_TRY(check_launch(c, "rbgs_half"));
+        rbgs_half<<<blocks, RB_THREADS, 0, c->stream>>>(a, 1);
+        PIC_TRY(check_launch(c, "rbgs_half"));
+    }
+    return PIC_OK;
+}
+
+static int rb_residual_async(pic_ctx* c, const RbArgs& a) {
+    rb_resid_partials<<<RB_RED_BLOCKS, RB_THREADS, 0, c->stream>>>(a, c->rb_partial);
+    PIC_TRY(check_launch(c, "rb_resid_partials"));
+    rb_final<<<1, RB_THREADS, 0, c->stream>>>(c->rb_partial, RB_RED_BLOCKS, 2, 0, c->rb_scalars + 1);
+    PIC_TRY(check_launch(c, "rb_final"));
+    rb_final<<<1, RB_THREADS, 0, c->stream>>>(c->rb_partial, RB_RED_BLOCKS, 2, 1, c->rb_scalars + 2);
+    return check_launch(c, "rb_final");
+}
+
+// rhs b = rho*dV - mean into c->rb_b (queued).
+static int rb_prepare(pic_ctx* c) {
+    const unsigned blocks = (unsigned)((c->G + 255) / 256);
+    rb_sum_rhs<<<RB_RED_BLOCKS, RB_THREADS, 0, c->stream>>>(c->rho, c->dx * c->dy, c->G, c->rb_partial);
+    PIC_TRY(check_launch(c, "rb_sum_rhs"));
+    rb_final<<<1, RB_THREADS, 0, c->stream>>>(c->rb_partial, RB_RED_BLOCKS, 1, 0, c->rb_scalars);
+    PIC_TRY(check_launch(c, "rb_final"));
+    rb_make_rhs<<<blocks, 256, 0, c->stream>>>(c->rho, c->dx * c->dy, c->G, c->rb_scalars, c->rb_b);
+    return check_launch(c, "rb_make_rhs");
+}
+
+static int rb_finish(pic_ctx* c) {
+    const unsigned blocks = (unsigned)((c->G + 255) / 256);
+    rb_sum_rhs<<<RB_RED_BLOCKS, RB_THREADS, 0, c->stream>>>(c->phi, 1.0, c->G, c->rb_partial);
+    PIC_TRY(check_launch(c, "rb_sum_rhs"));
+    rb_final<<<1, RB_THREADS, 0, c->stream>>>(c->rb_partial, RB_RED_BLOCKS, 1, 0, c->rb_scalars + 3);
+    PIC_TRY(check_launch(c, "rb_final"));
+    rb_sub_mean<<<blocks, 256, 0, c->stream>>>(c->phi, c->G, c->rb_scalars + 3);
+    PIC_TRY(check_launch(c, "rb_sub_mean"));
+    return efield_from_phi(c);
+}
+
+// Solves with the residual checked on the host every `check_every` sweeps.
+int rbgs_solve(pic_ctx* c, double tol, int max_iters, int check_every, int* iters_out, double* resid_out) {
+    if ((c->Nx & 1) || (c->Ny & 1)) return fail(PIC_ERR_UNSUPPORTED, "red-black Gauss-Seidel needs even Nx and Ny");
+    if (max_iters < 0) return fail(PIC_ERR_ARG, "max_iters < 0");
+    if (check_every < 1) check_every = 1;
+    PIC_TRY(ensure_rbgs(c));
+    PIC_TRY(rb_prepare(c));
+    const RbArgs a = rb_args(c);
+    int it = 0;
+    double res = 0.0;
+    prof_begin(c, "rbgs");
+    for (;;) {
+        PIC_TRY(rb_residual_async(c, a));
+        double s[3];
+        PIC_CUDA_TRY(cudaMemcpyAsync(s, c->rb_scalars, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
+        PIC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        res = s[2] > 0.0 ? std::sqrt(s[1] / s[2]) : std::sqrt(s[1]);
+        if (res <= tol || it >= max_iters) break;
+        const int n = (max_iters - it) < check_every ? (max_iters - it) : check_every;
+        PIC_TRY(rb_sweeps(c, a, n));
+        it += n;
+    }
+    prof_end(c);
+    PIC_TRY(rb_finish(c));
+    if (iters_out) *iters_out = it;
+    if (resid_out) *resid_out = res;
+    c->last_rbgs_iters = it;
+    c->last_rbgs_resid = res;
+    return PIC_OK;
+}
+
+int rbgs_solve_async(pic_ctx* c, double tol, int max_iters, int check_every) {
+    return rbgs_solve(c, tol, max_iters, check_every, nullptr, nullptr);
+}
+
+void release_rbgs(pic_ctx* c) {
+    dfree(c->rb_b);
+    dfree(c->rb_partial);
+    dfree(c->rb_scalars);
+}
+
+}  // namespace picgb
+
+using namespace picgb;
+
+extern "C" int pic_gpu_poisson_rbgs(pic_ctx* c, double tol, int max_iters, int warm_start, int check_every,
+                                    int* iters_out, double* resid_out) {
+    if (!c) return fail(PIC_ERR_ARG, "NULL context");
+    PIC_CUDA_TRY(cudaSetDevice(c->device));
+    PIC_TRY(ensure_fields(c));
+    if (!warm_start) PIC_CUDA_TRY(cudaMemsetAsync(c->phi, 0, c->G * 8, c->stream));
+    PIC_TRY(rbgs_solve(c, tol, max_iters, check_every, iters_out, resid_out));
+    return pic_gpu_synchronize(c);
+}

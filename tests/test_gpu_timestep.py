@@ -1,0 +1,137 @@
+"""Time stepping (pic_gpu_run) and red-black Gauss-Seidel through the C ABI.
+
+* The step loop against the oracle's FP64 restatement of Simulation::run
+  (src/pic/simulation.cpp:82-131): energies within 1e-4 over the first steps
+  (the GPU state is FP32 cell-relative, the oracle FP64).
+* The sort interval and CUDA-graph replay change no bit of the result (the
+  deposit is order independent).
+* Langmuir validation (src/pic/validation.cpp:200-261, the set-up of
+  src/main_validation.cpp:7-17): the dominant field-energy frequency bin equals
+  the reference's archived 0.1220703125 (data/benchmarks/validation.csv:2-5).
+* Conservation study set-up (main_validation.cpp:29-36): charge error stays at
+  round-off and the energy drift is small.
+* RBGS converges to the oracle's red-black solution; a warm start at the
+  solution takes no sweep.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NGP, CIC, TSC, ESK = 0, 1, 2, 3
+
+
+def start(pg, nx, ny, lx, ly, p):
+    c = pg.Context(nx, ny, lx, ly, len(p["x"]))
+    c.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+    return c
+
+
+@pytest.mark.parametrize("scheme", [NGP, CIC, TSC, ESK])
+def test_run_tracks_fp64_oracle(pg, port, oracle_mod, scheme):
+    nx = ny = 32
+    p = port.init_particles(0, nx, ny, 1.0, 1.0, 4000, p0=1.0, seed=42)
+    with start(pg, nx, ny, 1.0, 1.0, p) as c:
+        got = c.run(20, scheme=scheme, dt=0.005, sort_interval=5)
+    want, _ = oracle_mod.simulate(port, nx, ny, 1.0, 1.0, p, scheme, 0.005, 20)
+    for col in (3, 4, 5):  # kinetic, field, total
+        rel = np.max(np.abs(got[:, col] - want[:, col]) / np.abs(want[:, col]))
+        assert rel <= 1e-4, (col, rel)
+    assert np.max(got[:, 0]) <= 1e-12  # charge error (reference test: <= 1e-10)
+
+
+def test_sort_interval_and_graph_do_not_change_bits(pg, port):
+    nx = ny = 64
+    p = port.init_particles(0, nx, ny, 1.0, 1.0, 50000, p0=1.0, seed=3)
+    outs = []
+    for k, graph in ((0, False), (1, False), (7, True), (3, True)):
+        with start(pg, nx, ny, 1.0, 1.0, p) as c:
+            h = c.run(25, scheme=TSC, dt=0.004, sort_interval=k, use_graph=graph)
+            lay = c.device_layout()
+        # compare the particle state as a set (order differs with the sort interval)
+        key = np.lexsort((lay["vy"], lay["vx"], lay["yr"], lay["xr"], lay["cell"]))
+        outs.append((h, {kk: v[key] for kk, v in lay.items()}))
+    for h, lay in outs[1:]:
+        # particle state and every grid quantity are bit-identical ...
+        for kk in lay:
+            assert np.array_equal(lay[kk], outs[0][1][kk])
+        for col in (0, 1, 2, 4):  # charge error, total charge, integrated rho, field energy
+            assert np.array_equal(h[:, col], outs[0][0][:, col])
+        # ... the FP64 kinetic-energy sum runs over the particles in their current order
+        assert np.allclose(h[:, 3], outs[0][0][:, 3], rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("scheme", [NGP, CIC, TSC, ESK])
+def test_langmuir_frequency_bin(pg, port, oracle_mod, scheme):
+    # main_validation.cpp:7-17: 64x64, L=1, dt=0.002, 16384 steps, 200 particles,
+    # amplitude 0.05, mode 1; background 1/V (validation.cpp:56-61)
+    nx = ny = 64
+    steps = 16384
+    p = port.init_particles(1, nx, ny, 1.0, 1.0, 200, p0=0.05, mode=1, seed=42)
+    with start(pg, nx, ny, 1.0, 1.0, p) as c:
+        h = c.run(steps, scheme=scheme, dt=0.002, background=1.0, use_graph=True)
+    fe = h[steps // 4:, 4]
+    omega = oracle_mod.dominant_frequency(fe, 0.002)
+    assert omega == 0.1220703125  # data/benchmarks/validation.csv:2-5
+
+
+@pytest.mark.parametrize("scheme", [CIC, TSC])
+def test_conservation_study_setup(pg, port, scheme):
+    # main_validation.cpp:29-36: 64x64, L=1, dt=0.005, 2000 steps, 10000 particles
+    p = port.init_particles(0, 64, 64, 1.0, 1.0, 10000, p0=1.0, seed=42)
+    with start(pg, 64, 64, 1.0, 1.0, p) as c:
+        h = c.run(2000, scheme=scheme, dt=0.005, sort_interval=1, use_graph=True)
+    drift = (h[-1, 5] - h[0, 5]) / abs(h[0, 5])
+    assert np.max(h[:, 0]) <= 1e-12
+    # reference drifts (conservation_study.csv:3-4): CIC -1.8e-6, TSC -1.9e-5
+    assert abs(drift) <= 1e-4, drift
+
+
+def test_rbgs_matches_oracle(pg, port):
+    nx, ny = 64, 48
+    rng = np.random.default_rng(0)
+    rho = rng.normal(size=nx * ny)
+    with pg.Context(nx, ny, 6.4, 4.8, 1) as c:
+        c.set_rho(rho)
+        it, res = c.poisson_rbgs(tol=1e-10, max_iters=200000, warm_start=False, check_every=50)
+        phi, ex, ey = c.fields()
+        it2, res2 = c.poisson_rbgs(tol=1e-10, warm_start=True, check_every=50)
+    assert res <= 1e-10 and it > 0
+    assert it2 == 0 and res2 <= 1e-10
+    want, wit, wres = port.rbgs(nx, ny, 6.4, 4.8, rho, tol=1e-10, max_iters=200000, check_every=50)
+    assert abs(it - wit) <= 50
+    assert np.max(np.abs(phi - want)) <= 1e-8 * np.max(np.abs(want))
+    wex, wey = port.efield(nx, ny, 6.4, 4.8, phi)
+    assert np.array_equal(ex, wex) and np.array_equal(ey, wey)
+
+
+def test_rbgs_fixed_sweeps_close_to_oracle(pg, port):
+    nx, ny = 32, 32
+    rng = np.random.default_rng(1)
+    rho = rng.normal(size=nx * ny)
+    with pg.Context(nx, ny, 1.0, 1.0, 1) as c:
+        c.set_rho(rho)
+        it, _ = c.poisson_rbgs(tol=0.0, max_iters=37, warm_start=False, check_every=1000)
+        phi, _, _ = c.fields()
+    want, wit, _ = port.rbgs(nx, ny, 1.0, 1.0, rho, tol=0.0, max_iters=37, check_every=1000)
+    assert it == wit == 37
+    # same arithmetic per sweep; the mean of the right-hand side is summed in another order
+    assert np.max(np.abs(phi - want)) <= 1e-12 * np.max(np.abs(want))
+
+
+def test_rbgs_odd_grid_rejected(pg):
+    with pg.Context(33, 32, 1.0, 1.0, 1) as c:
+        c.set_rho(np.zeros(33 * 32))
+        with pytest.raises(pg.PicError) as e:
+            c.poisson_rbgs()
+        assert e.value.code == -8
+
+
+def test_run_with_rbgs_poisson(pg, port):
+    p = port.init_particles(0, 32, 32, 1.0, 1.0, 3000, p0=1.0, seed=5)
+    with start(pg, 32, 32, 1.0, 1.0, p) as c:
+        h_fft = c.run(5, scheme=CIC, dt=0.005)
+    with start(pg, 32, 32, 1.0, 1.0, p) as c:
+        h_gs = c.run(5, scheme=CIC, dt=0.005, poisson=1, rbgs_tol=1e-12, rbgs_max_iters=200000)
+    # FFT uses the continuous k^2, GS the 5-point Laplacian: same physics, different discretisation
+    assert np.allclose(h_gs[:, 3], h_fft[:, 3], rtol=1e-3)

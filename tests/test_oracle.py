@@ -202,3 +202,22 @@ def test_rbgs_matches_converged_lexicographic_gs(port):
     phi_gs, _, _, _ = port.gs_ref(32, 32, 1.0, 1.0, rho, 200000, 1e-15)
     phi_gs = phi_gs - phi_gs.mean()
     assert np.max(np.abs(phi_rb - phi_gs)) <= 1e-8 * np.max(np.abs(phi_gs))
+
+
+# ---- the oracle's time loop and frequency estimator vs the reference -------
+@pytest.mark.parametrize("scheme", [CIC, ESK])
+def test_simulate_matches_reference_simulation(port, ref, oracle_mod, scheme):
+    # Simulation::run (simulation.cpp:69-145) on a uniform Maxwellian, FFT Poisson
+    p = port.init_particles(0, 32, 32, 1.0, 1.0, 2000, p0=1.0, seed=42)
+    h, _ = oracle_mod.simulate(port, 32, 32, 1.0, 1.0, p, scheme, 0.005, 30)
+    r = ref.simulation_run(32, 32, 1.0, 1.0, 0.005, 30, scheme, 2000, seed=42, mode=0, temperature=1.0)
+    assert np.allclose(h[:, 5], r["total"], rtol=1e-10, atol=0)
+    assert np.allclose(h[:, 3], r["kinetic"], rtol=1e-10, atol=0)
+
+
+def test_dominant_frequency_matches_reference(port, ref, oracle_mod):
+    # runLangmuirValidation (validation.cpp:200-261) on a shortened run
+    out = ref.langmuir_validation(64, 64, 1.0, 1.0, 0.002, 2048, CIC, 200, amplitude=0.05, mode_number=1)
+    p = port.init_particles(1, 64, 64, 1.0, 1.0, 200, p0=0.05, mode=1, seed=42)
+    h, _ = oracle_mod.simulate(port, 64, 64, 1.0, 1.0, p, CIC, 0.002, 2048, background=1.0)
+    assert oracle_mod.dominant_frequency(h[2048 // 4:, 4], 0.002) == out["omega_measured"]
