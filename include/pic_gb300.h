@@ -150,6 +150,17 @@ int pic_gpu_deposit(pic_ctx* ctx, int scheme, double dt, double background, doub
 int pic_gpu_get_rho_fixed(pic_ctx* ctx, int64_t* acc_out, double* unit_out);
 int pic_gpu_get_rho(pic_ctx* ctx, double* rho_out);
 
+/* ---- Esirkepov current (new; the reference's "Esirkepov" deposits charge only,
+ *      src/deposition/ngp.cpp:13-84) ----
+ * First-order charge-conserving current (Esirkepov 2001) of the move x -> x + v*dt
+ * of every resident particle: Jx[iy*Nx+ix] on the edge from node (ix,iy) to
+ * (ix+1,iy), Jy[iy*Nx+ix] on the edge to (ix,iy+1). Needs |v|*dt < cell size on
+ * each axis (PIC_ERR_COURANT). In the int64 grids, the CIC charge after
+ * pic_gpu_push(dt) minus the charge before plus the integer divergence of J is
+ * exactly zero at every node. J unit = max|q|*inv_vol*2^-24*dx/dt (x), dy/dt (y). */
+int pic_gpu_deposit_current(pic_ctx* ctx, double dt, double* jx_out, double* jy_out);
+int pic_gpu_get_current_fixed(pic_ctx* ctx, int64_t* jx, int64_t* jy, double* unit_x, double* unit_y);
+
 /* ---- fields: pic::FieldGrid (src/pic/field_grid.hpp:9-39) ---- */
 
 /* Replaces FieldGrid::rho() with caller data (Nx*Ny doubles). */

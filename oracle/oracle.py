@@ -88,6 +88,9 @@ class Port:
         L.orc_deposit_fixed.argtypes = [D, C.c_int, C.c_size_t, _u32p, _fp, _fp, _fp, _fp, _fp, C.c_float, C.c_double,
                                         _i64p, C.POINTER(C.c_double)]
         L.orc_fixed_to_rho.argtypes = [C.c_size_t, _i64p, C.c_double, C.c_double, _dp]
+        L.orc_esirkepov_j_ref.argtypes = [D, C.c_size_t, _dp, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp]
+        L.orc_esirkepov_j_fixed.argtypes = [D, C.c_size_t, _u32p, _fp, _fp, _fp, _fp, _fp, C.c_float, C.c_double,
+                                            _i64p, _i64p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_move_f32.argtypes = [D, C.c_size_t, _u32p, _fp, _fp, _fp, _fp, _fp, C.c_float, C.c_void_p, _dp, _dp,
                                    C.c_double, C.c_int, C.c_int]
 
@@ -210,6 +213,26 @@ class Port:
                                         _c(qn, np.float32), float(maxq), dt, acc, C.byref(unit))
         assert rc == 0
         return acc, unit.value
+
+    def esirkepov_j_ref(self, nx, ny, lx, ly, p, dt):
+        """FP64 Esirkepov (CIC shape) current: (Jx, Jy) at the x / y cell edges."""
+        jx, jy = np.zeros(nx * ny), np.zeros(nx * ny)
+        rc = self.lib.orc_esirkepov_j_ref(self.dom(nx, ny, lx, ly), len(p["x"]), _c(p["x"], np.float64),
+                                          _c(p["y"], np.float64), _c(p["vx"], np.float64), _c(p["vy"], np.float64),
+                                          _c(p["q"], np.float64), dt, jx, jy)
+        assert rc == 0, "Courant violated"
+        return jx, jy
+
+    def esirkepov_j_fixed(self, nx, ny, lx, ly, lay, maxq, dt):
+        """The GPU's integer current on the device layout: (jx, jy, unit_x, unit_y)."""
+        jx, jy = np.zeros(nx * ny, np.int64), np.zeros(nx * ny, np.int64)
+        ux, uy = C.c_double(), C.c_double()
+        rc = self.lib.orc_esirkepov_j_fixed(self.dom(nx, ny, lx, ly), len(lay["cell"]), _c(lay["cell"], np.uint32),
+                                            _c(lay["xr"], np.float32), _c(lay["yr"], np.float32),
+                                            _c(lay["vx"], np.float32), _c(lay["vy"], np.float32),
+                                            _c(lay["q"], np.float32), float(maxq), dt, jx, jy, C.byref(ux), C.byref(uy))
+        assert rc == 0, "Courant violated"
+        return jx, jy, ux.value, uy.value
 
     def move_f32(self, nx, ny, lx, ly, lay, maxq, ex, ey, dt, gather=True, push=True, m=None):
         """The GPU's FP32 gather/push on a copy of the device layout `lay`."""

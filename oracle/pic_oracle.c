@@ -900,3 +900,171 @@ void orc_move_f32(const orc_domain* d, size_t n, uint32_t* cell, float* xr, floa
         }
     }
 }
+
+/* ======================================================================= */
+/* Esirkepov current (new; no reference implementation).                   */
+/* First-order (CIC-shape) charge-conserving current of Esirkepov, Comput. */
+/* Phys. Commun. 135 (2001) 144, in 2D: with S0, S1 the CIC weights of the */
+/* old and new positions and DS = S1 - S0 on a 4-node frame (cell offsets  */
+/* -1..2 around the old cell),                                             */
+/*   W1[j][i] = DSx[i] (S0y[j] + DSy[j]/2),  W2[j][i] = DSy[j] (S0x[i] + DSx[i]/2) */
+/*   Jx(i+1/2, j) = -q/dV dx/dt sum_{i'<=i} W1[j][i'],  Jy likewise in j.  */
+/* (a) FP64 restatement: orc_esirkepov_j_ref.                              */
+/* (b) restatement of the GPU fixed point: orc_esirkepov_j_fixed. Per       */
+/*     particle, R0/R1 are the integer CIC charges of the old/new position  */
+/*     (same rounding and remainder rule as the charge deposit), W1 is      */
+/*     rounded with row sums forced to 0 and column sums forced to those of */
+/*     R1-R0, W2 = (R1-R0) - W1, so (R1-R0) + div J = 0 holds exactly in    */
+/*     integers. J unit = max|q| inv_vol 2^-24 dx/dt (x) or dy/dt (y).      */
+/* Both require |v dt| < cell size on each axis.                           */
+/* ======================================================================= */
+
+/* S0 and DS = S1 - S0 on the 4-node frame from the in-cell offset r and the
+ * displacement d (|d| < 1), each DS entry formed from quantities of its own
+ * size (no cancellation of S1 - S0): no crossing DS = (0,-d,d,0); crossing
+ * up (fr = r+d-1) DS = (0, r-1, (1-r)-fr, fr); crossing down (e = r+d < 0)
+ * DS = (-e, r+e, -r, 0). */
+static void esk_ds(float r, float d, float* s0, float* ds) {
+    const float e = r + d;
+    const float f = floorf(e);
+    const float fr = e - f;
+    s0[0] = 0.0f; s0[1] = 1.0f - r; s0[2] = r; s0[3] = 0.0f;
+    if (f == 0.0f) {
+        ds[0] = 0.0f; ds[1] = -d; ds[2] = d; ds[3] = 0.0f;
+    } else if (f > 0.0f) {
+        ds[0] = 0.0f; ds[1] = r - 1.0f; ds[2] = (1.0f - r) - fr; ds[3] = fr;
+    } else {
+        ds[0] = -e; ds[1] = r + e; ds[2] = -r; ds[3] = 0.0f;
+    }
+}
+
+int orc_esirkepov_j_ref(const orc_domain* d, size_t n, const double* x, const double* y, const double* vx,
+                        const double* vy, const double* q, double dt, double* jx, double* jy) {
+    const int Nx = d->Nx, Ny = d->Ny;
+    const double dx = dom_dx(d), dy = dom_dy(d);
+    const double inv_vol = 1.0 / (dx * dy);
+    const size_t g = (size_t)Nx * Ny;
+    memset(jx, 0, g * sizeof(double));
+    memset(jy, 0, g * sizeof(double));
+    for (size_t p = 0; p < n; ++p) {
+        int ix, iy;
+        double rx, ry;
+        orc_cell_coords(d, x[p], y[p], &ix, &iy, &rx, &ry);
+        const double ddx = vx[p] * dt / dx, ddy = vy[p] * dt / dy;
+        if (!(fabs(ddx) < 1.0 && fabs(ddy) < 1.0)) return -1;
+        double S0x[4] = {0, 1 - rx, rx, 0}, S0y[4] = {0, 1 - ry, ry, 0};
+        double S1x[4] = {0, 0, 0, 0}, S1y[4] = {0, 0, 0, 0};
+        const double ex = rx + ddx, ey = ry + ddy;
+        const int kx = (int)floor(ex) + 1, ky = (int)floor(ey) + 1;
+        S1x[kx] = 1 - (ex - floor(ex));
+        S1x[kx + 1] = ex - floor(ex);
+        S1y[ky] = 1 - (ey - floor(ey));
+        S1y[ky + 1] = ey - floor(ey);
+        double DSx[4], DSy[4];
+        for (int i = 0; i < 4; ++i) {
+            DSx[i] = S1x[i] - S0x[i];
+            DSy[i] = S1y[i] - S0y[i];
+        }
+        const double cx = q[p] * inv_vol * dx / dt, cy = q[p] * inv_vol * dy / dt;
+        for (int j = 0; j < 4; ++j) {
+            double cum = 0.0;
+            for (int i = 0; i < 3; ++i) {
+                cum += DSx[i] * (S0y[j] + 0.5 * DSy[j]);
+                jx[(size_t)wrap_index(iy - 1 + j, Ny) * Nx + wrap_index(ix - 1 + i, Nx)] += -cx * cum;
+            }
+        }
+        for (int i = 0; i < 4; ++i) {
+            double cum = 0.0;
+            for (int j = 0; j < 3; ++j) {
+                cum += DSy[j] * (S0x[i] + 0.5 * DSx[i]);
+                jy[(size_t)wrap_index(iy - 1 + j, Ny) * Nx + wrap_index(ix - 1 + i, Nx)] += -cy * cum;
+            }
+        }
+    }
+    return 0;
+}
+
+/* integer CIC charges of a particle on the 4x4 frame; node (k, k+1) per axis */
+static void cic_frame_int(float a, int A, float rx, float ry, int kx, int ky, int64_t R[4][4]) {
+    const float X[2] = {1.0f - rx, rx}, Y[2] = {1.0f - ry, ry};
+    int v[2][2], sum = 0;
+    for (int j = 0; j < 2; ++j) {
+        const float ay = a * Y[j];
+        for (int i = 0; i < 2; ++i) {
+            v[j][i] = fixed_rn(ay * X[i]);
+            sum += v[j][i];
+        }
+    }
+    const int mx = X[1] > X[0] ? 1 : 0, my = Y[1] > Y[0] ? 1 : 0;
+    v[my][mx] += A - sum;
+    for (int j = 0; j < 4; ++j)
+        for (int i = 0; i < 4; ++i) R[j][i] = 0;
+    for (int j = 0; j < 2; ++j)
+        for (int i = 0; i < 2; ++i) R[ky + j][kx + i] = v[j][i];
+}
+
+int orc_esirkepov_j_fixed(const orc_domain* d, size_t n, const uint32_t* cell, const float* xr, const float* yr,
+                          const float* vx, const float* vy, const float* qn, float maxq, double dt, int64_t* jx,
+                          int64_t* jy, double* unit_x, double* unit_y) {
+    const int Nx = d->Nx, Ny = d->Ny;
+    const size_t g = (size_t)Nx * Ny;
+    memset(jx, 0, g * sizeof(int64_t));
+    memset(jy, 0, g * sizeof(int64_t));
+    const double dx = dom_dx(d), dy = dom_dy(d);
+    const double inv_vol = 1.0 / (dx * dy);
+    const double unit = ((double)maxq * inv_vol) * 5.9604644775390625e-08;
+    if (unit_x) *unit_x = unit * (dx / dt);
+    if (unit_y) *unit_y = unit * (dy / dt);
+    const float dtdx = (float)(dt / dx), dtdy = (float)(dt / dy);
+    for (size_t p = 0; p < n; ++p) {
+        const int ix = (int)(cell[p] % (uint32_t)Nx), iy = (int)(cell[p] / (uint32_t)Nx);
+        const float ddx = vx[p] * dtdx, ddy = vy[p] * dtdy;
+        if (!(fabsf(ddx) < 1.0f && fabsf(ddy) < 1.0f)) return -1;
+        float s0x[4], dsx[4], s0y[4], dsy[4];
+        esk_ds(xr[p], ddx, s0x, dsx);
+        esk_ds(yr[p], ddy, s0y, dsy);
+        const float a = qn[p] * 16777216.0f;
+        const int A = fixed_rn(a);
+        /* old / new integer charges */
+        int64_t R0[4][4], R1[4][4];
+        cic_frame_int(a, A, xr[p], yr[p], 1, 1, R0);
+        const float ex = xr[p] + ddx, ey = yr[p] + ddy;
+        const float fx = floorf(ex), fy = floorf(ey);
+        cic_frame_int(a, A, ex - fx, ey - fy, (int)fx + 1, (int)fy + 1, R1);
+        int64_t dR[4][4], W1[4][4], colR[4] = {0, 0, 0, 0};
+        for (int j = 0; j < 4; ++j)
+            for (int i = 0; i < 4; ++i) {
+                dR[j][i] = R1[j][i] - R0[j][i];
+                colR[i] += dR[j][i];
+            }
+        for (int j = 0; j < 3; ++j) {
+            const float ay = a * (s0y[j] + 0.5f * dsy[j]);
+            int64_t row = 0;
+            for (int i = 0; i < 3; ++i) {
+                W1[j][i] = fixed_rn(ay * dsx[i]);
+                row += W1[j][i];
+            }
+            W1[j][3] = -row;
+        }
+        for (int i = 0; i < 4; ++i) {
+            int64_t col = 0;
+            for (int j = 0; j < 3; ++j) col += W1[j][i];
+            W1[3][i] = colR[i] - col;
+        }
+        for (int j = 0; j < 4; ++j) {
+            int64_t cum = 0;
+            for (int i = 0; i < 3; ++i) {
+                cum += W1[j][i];
+                jx[(size_t)wrap_index(iy - 1 + j, Ny) * Nx + wrap_index(ix - 1 + i, Nx)] -= cum;
+            }
+        }
+        for (int i = 0; i < 4; ++i) {
+            int64_t cum = 0;
+            for (int j = 0; j < 3; ++j) {
+                cum += dR[j][i] - W1[j][i];
+                jy[(size_t)wrap_index(iy - 1 + j, Ny) * Nx + wrap_index(ix - 1 + i, Nx)] -= cum;
+            }
+        }
+    }
+    return 0;
+}

@@ -79,6 +79,11 @@ int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t*
                       const float* yr, const float* vx, const float* vy, const float* qn, float maxq, double dt,
                       int64_t* acc, double* unit_out);
 void orc_fixed_to_rho(size_t g, const int64_t* acc, double unit, double background, double* rho);
+int orc_esirkepov_j_ref(const orc_domain* d, size_t n, const double* x, const double* y, const double* vx,
+                        const double* vy, const double* q, double dt, double* jx, double* jy);
+int orc_esirkepov_j_fixed(const orc_domain* d, size_t n, const uint32_t* cell, const float* xr, const float* yr,
+                          const float* vx, const float* vy, const float* qn, float maxq, double dt, int64_t* jx,
+                          int64_t* jy, double* unit_x, double* unit_y);
 void orc_move_f32(const orc_domain* d, size_t n, uint32_t* cell, float* xr, float* yr, float* vx, float* vy,
                   const float* qn, float maxq, const float* m, const double* Ex, const double* Ey, double dt,
                   int gather, int push);

@@ -366,6 +366,7 @@ int pic_gpu_destroy(pic_ctx* c) {
     for (void* p : ptrs) dfree(p);
     release_fields(c);
     release_rbgs(c);
+    release_current(c);
     prof_clear(c, nullptr);
     delete c->prof;
     if (c->stream) cudaStreamDestroy(c->stream);

@@ -96,6 +96,10 @@ struct pic_ctx {
     double *rb_b = nullptr, *rb_partial = nullptr, *rb_scalars = nullptr;
     int last_rbgs_iters = 0;
     double last_rbgs_resid = 0.0;
+    // Esirkepov current: int64 edge grids, FP64 copies, units (x, y)
+    long long *accjx = nullptr, *accjy = nullptr;
+    double *jx = nullptr, *jy = nullptr, *junits = nullptr;
+    int has_current = 0;
     // kernels inside the captured time-step graphs (for the launch counter)
     long long graph_launches_sort = 0, graph_launches_plain = 0;
 
@@ -147,6 +151,7 @@ int diagnostics_async(pic_ctx* ctx);
 int read_diagnostics(pic_ctx* ctx, pic_diag* d);
 void release_fields(pic_ctx* ctx);
 void release_rbgs(pic_ctx* ctx);
+void release_current(pic_ctx* ctx);
 // Deposit (deposit.cu).
 int deposit_rho(pic_ctx* ctx, int scheme, double dt, double background);
 

@@ -17,6 +17,8 @@
 // are reduced and finalised on the device into a history buffer, read back once
 // at the end. With use_graph, one eager step warms every allocation, then the
 // step with and without the sort are captured as CUDA graphs and replayed.
+#include <vector>
+
 #include "pic_internal.cuh"
 
 namespace picgb {
@@ -64,6 +66,62 @@ static int one_step(pic_ctx* c, const pic_run_config* cfg, bool do_sort, double*
     return check_launch(c, "finalize_diag");
 }
 
+// The cell sort ping-pongs the particle arrays with their scratch copies by
+// swapping the context's pointers on the host. A captured graph keeps the
+// pointers of its capture, so each graph is keyed by the buffer assignment it
+// starts from and records the assignment it leaves; after a replay the host
+// pointers are set to that assignment. Assignments alternate between two
+// states, so at most four graphs exist.
+struct Buffers {
+    uint32_t *cell, *cell_alt, *idx_a, *idx_b;
+    float *xr, *yr, *vx, *vy, *q, *m;
+    float* alt[6];
+    int sorted;
+    bool operator==(const Buffers& o) const {
+        return cell == o.cell && cell_alt == o.cell_alt && idx_a == o.idx_a && xr == o.xr && yr == o.yr &&
+               vx == o.vx && vy == o.vy && q == o.q && m == o.m;
+    }
+};
+
+static Buffers buffers_of(const pic_ctx* c) {
+    Buffers b;
+    b.cell = c->cell;
+    b.cell_alt = c->cell_alt;
+    b.idx_a = c->idx_a;
+    b.idx_b = c->idx_b;
+    b.xr = c->xr;
+    b.yr = c->yr;
+    b.vx = c->vx;
+    b.vy = c->vy;
+    b.q = c->q;
+    b.m = c->m;
+    for (int k = 0; k < 6; ++k) b.alt[k] = c->alt[k];
+    b.sorted = c->sorted;
+    return b;
+}
+
+static void set_buffers(pic_ctx* c, const Buffers& b) {
+    c->cell = b.cell;
+    c->cell_alt = b.cell_alt;
+    c->idx_a = b.idx_a;
+    c->idx_b = b.idx_b;
+    c->xr = b.xr;
+    c->yr = b.yr;
+    c->vx = b.vx;
+    c->vy = b.vy;
+    c->q = b.q;
+    c->m = b.m;
+    for (int k = 0; k < 6; ++k) c->alt[k] = b.alt[k];
+    c->sorted = b.sorted;
+}
+
+struct StepGraph {
+    bool do_sort;
+    Buffers before, after;
+    cudaGraphExec_t exec;
+    long long kernels;
+};
+
 static int capture(pic_ctx* c, const pic_run_config* cfg, bool do_sort, double* hist, int* ctr, int steps,
                    cudaGraphExec_t* out) {
     const int prof = c->prof_enabled;
@@ -100,10 +158,9 @@ int run_steps(pic_ctx* c, const pic_run_config* cfg, int steps, pic_diag* histor
         dfree(hist);
         return rc;
     }
-    cudaGraphExec_t gsort = nullptr, gplain = nullptr;
+    std::vector<StepGraph> graphs;
     auto cleanup = [&]() {
-        if (gsort) cudaGraphExecDestroy(gsort);
-        if (gplain) cudaGraphExecDestroy(gplain);
+        for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
         cudaStreamSynchronize(c->stream);
         dfree(hist);
         dfree(ctr);
@@ -120,10 +177,23 @@ int run_steps(pic_ctx* c, const pic_run_config* cfg, int steps, pic_diag* histor
                 PIC_TRY(one_step(c, cfg, do_sort, hist, ctr, steps));
                 continue;
             }
-            cudaGraphExec_t& g = do_sort ? gsort : gplain;
-            if (!g) PIC_TRY(capture(c, cfg, do_sort, hist, ctr, steps, &g));
-            PIC_CUDA_TRY(cudaGraphLaunch(g, c->stream));
-            c->launches += do_sort ? c->graph_launches_sort : c->graph_launches_plain;
+            const Buffers now = buffers_of(c);
+            StepGraph* g = nullptr;
+            for (auto& sg : graphs)
+                if (sg.do_sort == do_sort && sg.before == now && sg.before.sorted == now.sorted) g = &sg;
+            if (!g) {
+                StepGraph sg;
+                sg.do_sort = do_sort;
+                sg.before = now;
+                PIC_TRY(capture(c, cfg, do_sort, hist, ctr, steps, &sg.exec));
+                sg.after = buffers_of(c);  // the capture ran the host side: pointers as the graph leaves them
+                sg.kernels = do_sort ? c->graph_launches_sort : c->graph_launches_plain;
+                graphs.push_back(sg);
+                g = &graphs.back();
+            }
+            PIC_CUDA_TRY(cudaGraphLaunch(g->exec, c->stream));
+            set_buffers(c, g->after);
+            c->launches += g->kernels;
         }
         if (history)
             PIC_CUDA_TRY(cudaMemcpyAsync(history, hist, (size_t)steps * 6 * sizeof(double), cudaMemcpyDeviceToHost,

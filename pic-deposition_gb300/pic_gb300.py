@@ -96,6 +96,8 @@ class RunConfig(C.Structure):
 
 
 _SIGS.append(("pic_gpu_run", [_vp, C.POINTER(RunConfig), C.c_int, C.POINTER(_Diag)]))
+_SIGS.append(("pic_gpu_deposit_current", [_vp, C.c_double, _vp, _vp]))
+_SIGS.append(("pic_gpu_get_current_fixed", [_vp, _vp, _vp, _dp, _dp]))
 
 
 class PinnedArray:
@@ -281,6 +283,18 @@ class Context:
 
     def gather_push(self, dt):
         _check(lib().pic_gpu_gather_push(self.h, float(dt)))
+
+    def deposit_current(self, dt, download=True):
+        jx = np.zeros(self.G) if download else None
+        jy = np.zeros(self.G) if download else None
+        _check(lib().pic_gpu_deposit_current(self.h, float(dt), _ptr(jx), _ptr(jy)))
+        return jx, jy
+
+    def current_fixed(self):
+        jx, jy = np.zeros(self.G, np.int64), np.zeros(self.G, np.int64)
+        ux, uy = C.c_double(), C.c_double()
+        _check(lib().pic_gpu_get_current_fixed(self.h, _ptr(jx), _ptr(jy), C.byref(ux), C.byref(uy)))
+        return jx, jy, ux.value, uy.value
 
     def poisson_rbgs(self, tol=1e-8, max_iters=1_000_000, warm_start=True, check_every=64):
         it = C.c_int()
