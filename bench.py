@@ -344,6 +344,44 @@ def run_gpu(args, d: Dist):
                                   "kernel_gbs": (bpp * n + BYTES_PER_CELL * G) / (kms / 1e3) / 1e9}
     extras["sort_random_to_cells"] = {"ms": sort_ms, "particles_per_s": n / (sort_ms / 1e3),
                                       "algorithmic_gbs": (48 * n + 4 * (G + 1)) / (sort_ms / 1e3) / 1e9}
+    # Esirkepov current of the sorted particles (24 B/particle + 2 x 8 B/cell)
+    for _ in range(2):
+        ctx.deposit_current(ESK_DT, download=False)
+    ctx.profile_read("current")
+    for _ in range(10):
+        ctx.deposit_current(ESK_DT, download=False)
+    ms, cnt = ctx.profile_read("current")
+    extras["Esirkepov_current_sorted"] = {"particles_per_s": n / (ms / cnt / 1e3), "kernel_ms": ms / cnt,
+                                          "kernel_gbs": (24 * n + 16 * G) / (ms / cnt / 1e3) / 1e9}
+    # FFT Poisson on the 1024^2 grid (cuFFT D2Z + k-divide + Z2D), neutral rho
+    ctx.deposit(SCHEMES["CIC"], ESK_DT, background=float(PPC), download=False)
+    for _ in range(2):
+        ctx.poisson_fft()
+    ctx.profile_read("poisson_fft")
+    for _ in range(10):
+        ctx.poisson_fft()
+    ms, cnt = ctx.profile_read("poisson_fft")
+    extras["poisson_fft_1024x1024"] = {"ms": ms / cnt}
+    # fused gather + push (44 B/particle + 2 x 4 B/cell FP32 fields)
+    for _ in range(2):
+        ctx.gather_push(0.0)
+    ctx.profile_read("gather_push")
+    for _ in range(10):
+        ctx.gather_push(0.0)
+    ms, cnt = ctx.profile_read("gather_push")
+    extras["gather_push"] = {"particles_per_s": n / (ms / cnt / 1e3), "kernel_ms": ms / cnt,
+                             "kernel_gbs": (44 * n + 8 * G) / (ms / cnt / 1e3) / 1e9}
+    # full time step: push, [sort every 10], TSC deposit + background, FFT Poisson,
+    # gather, FP64 diagnostics; CUDA-graph replay; host wall time per step
+    ctx.run(3, scheme=SCHEMES["TSC"], dt=ESK_DT, background=float(PPC), sort_interval=10, use_graph=True)
+    t0 = time.perf_counter()
+    ctx.run(20, scheme=SCHEMES["TSC"], dt=ESK_DT, background=float(PPC), sort_interval=10, use_graph=True)
+    extras["timestep_tsc_sort10"] = {"ms_per_step": (time.perf_counter() - t0) * 1e3 / 20,
+                                     "particles_per_s": n * 20 / (time.perf_counter() - t0)}
+    # restore the benchmark state: the random-order particles, cell-sorted
+    ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+    ctx.sort()
+    assert ctx.is_sorted()
 
     # ---- timed region: K deposits of the sorted particles ----
     for _ in range(args.warmup):

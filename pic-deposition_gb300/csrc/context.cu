@@ -207,9 +207,10 @@ int exclusive_scan_u32(pic_ctx* ctx, unsigned int* data, size_t n) {
 // upload: FP64 host SoA -> device cell key + FP32 in-cell offsets
 // ---------------------------------------------------------------------------
 struct ConvertArgs {
-    const double *x, *y, *vx, *vy, *q, *m;  // staged chunk (device); vx/vy/m may be null
+    const double *x, *y, *vx, *vy, *q, *m;  // chunk (device staging or pinned host); vx/vy/m may be null
     size_t count, first;                    // chunk size and global index of its first particle
     double dx, dy;
+    double inv_dx, inv_dy;                  // exact reciprocals when dx / dy are powers of two, else 0
     int Nx, Ny;
     uint32_t* cell;
     float *xr, *yr, *fvx, *fvy, *fq, *fm;
@@ -217,11 +218,12 @@ struct ConvertArgs {
 };
 
 // Domain::cellCoords (src/pic/domain.hpp:34-43) in FP64: w = x/dx, i = floor(w),
-// frac = w - i, i wrapped. The FP32 offset keeps the NGP choice frac >= 0.5
-// (ngp.cpp:116-117) exact: a frac below 0.5 that rounds up to 0.5f is stored
-// as the float just below 0.5.
-__device__ __forceinline__ bool cell_coord(double x, double d, int n, int* idx, float* off) {
-    const double w = __ddiv_rn(x, d);
+// frac = w - i, i wrapped. When dx is a power of two, x * (1/dx) equals the
+// correctly rounded x/dx exactly and replaces the (slow) FP64 division. The
+// FP32 offset keeps the NGP choice frac >= 0.5 (ngp.cpp:116-117) exact: a frac
+// below 0.5 that rounds up to 0.5f is stored as the float just below 0.5.
+__device__ __forceinline__ bool cell_coord(double x, double d, double inv_d, int n, int* idx, float* off) {
+    const double w = inv_d != 0.0 ? __dmul_rn(x, inv_d) : __ddiv_rn(x, d);
     if (!(fabs(w) < 1073741824.0)) return false;  // also rejects NaN/inf
     const double f = floor(w);
     int i = (int)f;
@@ -239,8 +241,8 @@ __global__ void convert_particles(ConvertArgs a) {
     if (i < a.count) {
         int ix = 0, iy = 0;
         float rx = 0.0f, ry = 0.0f;
-        const bool okx = cell_coord(a.x[i], a.dx, a.Nx, &ix, &rx);
-        const bool oky = cell_coord(a.y[i], a.dy, a.Ny, &iy, &ry);
+        const bool okx = cell_coord(a.x[i], a.dx, a.inv_dx, a.Nx, &ix, &rx);
+        const bool oky = cell_coord(a.y[i], a.dy, a.inv_dy, a.Ny, &iy, &ry);
         if (!(okx && oky)) set_dev_error(a.st, DEV_BAD_POSITION, (unsigned int)(a.first + i));
         const size_t o = a.first + i;
         a.cell[o] = (uint32_t)iy * (uint32_t)a.Nx + (uint32_t)ix;
@@ -268,6 +270,23 @@ __global__ void convert_particles(ConvertArgs a) {
         atomicMax(&a.st->maxvx_bits, __float_as_uint(avx));
         atomicMax(&a.st->maxvy_bits, __float_as_uint(avy));
     }
+}
+
+// 1/d when d is a power of two (then x * (1/d) == x / d exactly), else 0.
+static double exact_reciprocal(double d) {
+    int e = 0;
+    const double mant = std::frexp(d, &e);
+    return mant == 0.5 ? std::ldexp(1.0, 1 - e) : 0.0;
+}
+
+static int ensure_copy_stream(pic_ctx* c) {
+    if (c->copy_stream) return PIC_OK;
+    PIC_CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+        PIC_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_copied[k], cudaEventDisableTiming));
+        PIC_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_converted[k], cudaEventDisableTiming));
+    }
+    return PIC_OK;
 }
 
 // q <- q / max|q| (FP32 IEEE division): a uniform |q| becomes exactly +-1.
@@ -369,6 +388,14 @@ int pic_gpu_destroy(pic_ctx* c) {
     release_current(c);
     prof_clear(c, nullptr);
     delete c->prof;
+    for (int k = 0; k < 2; ++k) {
+        if (c->ev_copied[k]) cudaEventDestroy(c->ev_copied[k]);
+        if (c->ev_converted[k]) cudaEventDestroy(c->ev_converted[k]);
+    }
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return PIC_OK;
@@ -419,54 +446,91 @@ int pic_gpu_upload_particles(pic_ctx* c, const double* x, const double* y, const
     }
     c->has_mass = need_m ? 1 : 0;
 
-    // staging: chunks of up to 4M particles, 6 FP64 streams each
-    const size_t chunk = n < ((size_t)1 << 22) ? (n ? n : 1) : ((size_t)1 << 22);
-    if (c->stage_elems < chunk * 6) {
-        dfree(c->stage);
-        int rc;
-        c->stage = (double*)dalloc(chunk * 6 * sizeof(double), &rc);
-        if (!c->stage) {
-            c->stage_elems = 0;
-            return rc;
-        }
-        c->stage_elems = chunk * 6;
-    }
+    const double* src[6] = {x, y, vx, vy, q, need_m ? m : nullptr};
+    ConvertArgs a{};
+    a.dx = c->dx;
+    a.dy = c->dy;
+    a.inv_dx = exact_reciprocal(c->dx);
+    a.inv_dy = exact_reciprocal(c->dy);
+    a.Nx = c->Nx;
+    a.Ny = c->Ny;
+    a.cell = c->cell;
+    a.xr = c->xr;
+    a.yr = c->yr;
+    a.fvx = c->vx;
+    a.fvy = c->vy;
+    a.fq = c->q;
+    a.fm = need_m ? c->m : nullptr;
+    a.st = c->dstats;
     PIC_CUDA_TRY(cudaMemsetAsync(c->dstats, 0, sizeof(DevStats), c->stream));
-    for (size_t first = 0; first < n; first += chunk) {
-        const size_t cnt = (n - first) < chunk ? (n - first) : chunk;
-        double* s = c->stage;
-        const double* src[6] = {x, y, vx, vy, q, need_m ? m : nullptr};
-        double* dst[6];
-        for (int k = 0; k < 6; ++k) {
-            dst[k] = s + (size_t)k * chunk;
-            if (src[k])
-                PIC_CUDA_TRY(cudaMemcpyAsync(dst[k], src[k] + first, cnt * sizeof(double), cudaMemcpyHostToDevice,
-                                             c->stream));
+
+    // Page-locked inputs are read by the conversion kernel itself over the
+    // host link (one pass, no staging copy); other inputs go through two device
+    // staging slots, the copy of chunk i+1 overlapping the conversion of chunk i.
+    const double* dev_src[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool direct = n > 0;
+    for (int k = 0; k < 6 && direct; ++k) {
+        if (!src[k]) continue;
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, src[k]) != cudaSuccess || at.type != cudaMemoryTypeHost ||
+            !at.devicePointer) {
+            (void)cudaGetLastError();
+            direct = false;
+        } else {
+            dev_src[k] = (const double*)at.devicePointer;
         }
-        ConvertArgs a;
-        a.x = dst[0];
-        a.y = dst[1];
-        a.vx = vx ? dst[2] : nullptr;
-        a.vy = vy ? dst[3] : nullptr;
-        a.q = dst[4];
-        a.m = need_m ? dst[5] : nullptr;
-        a.count = cnt;
-        a.first = first;
-        a.dx = c->dx;
-        a.dy = c->dy;
-        a.Nx = c->Nx;
-        a.Ny = c->Ny;
-        a.cell = c->cell;
-        a.xr = c->xr;
-        a.yr = c->yr;
-        a.fvx = c->vx;
-        a.fvy = c->vy;
-        a.fq = c->q;
-        a.fm = need_m ? c->m : nullptr;
-        a.st = c->dstats;
-        const unsigned blocks = (unsigned)((cnt + 255) / 256);
-        convert_particles<<<blocks, 256, 0, c->stream>>>(a);
+    }
+    if (direct) {
+        a.x = dev_src[0];
+        a.y = dev_src[1];
+        a.vx = dev_src[2];
+        a.vy = dev_src[3];
+        a.q = dev_src[4];
+        a.m = dev_src[5];
+        a.count = n;
+        a.first = 0;
+        convert_particles<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(a);
         PIC_TRY(check_launch(c, "convert_particles"));
+    } else if (n > 0) {
+        const size_t chunk = n < ((size_t)1 << 22) ? n : ((size_t)1 << 22);
+        if (c->stage_elems < chunk * 12) {
+            dfree(c->stage);
+            int rc;
+            c->stage = (double*)dalloc(chunk * 12 * sizeof(double), &rc);
+            if (!c->stage) {
+                c->stage_elems = 0;
+                return rc;
+            }
+            c->stage_elems = chunk * 12;
+        }
+        PIC_TRY(ensure_copy_stream(c));
+        int i = 0;
+        for (size_t first = 0; first < n; first += chunk, ++i) {
+            const int slot = i & 1;
+            const size_t cnt = (n - first) < chunk ? (n - first) : chunk;
+            double* s = c->stage + (size_t)slot * chunk * 6;
+            if (i >= 2) PIC_CUDA_TRY(cudaStreamWaitEvent(c->copy_stream, c->ev_converted[slot], 0));
+            double* dst[6];
+            for (int k = 0; k < 6; ++k) {
+                dst[k] = s + (size_t)k * chunk;
+                if (src[k])
+                    PIC_CUDA_TRY(cudaMemcpyAsync(dst[k], src[k] + first, cnt * sizeof(double),
+                                                 cudaMemcpyHostToDevice, c->copy_stream));
+            }
+            PIC_CUDA_TRY(cudaEventRecord(c->ev_copied[slot], c->copy_stream));
+            PIC_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_copied[slot], 0));
+            a.x = dst[0];
+            a.y = dst[1];
+            a.vx = vx ? dst[2] : nullptr;
+            a.vy = vy ? dst[3] : nullptr;
+            a.q = dst[4];
+            a.m = need_m ? dst[5] : nullptr;
+            a.count = cnt;
+            a.first = first;
+            convert_particles<<<(unsigned)((cnt + 255) / 256), 256, 0, c->stream>>>(a);
+            PIC_TRY(check_launch(c, "convert_particles"));
+            PIC_CUDA_TRY(cudaEventRecord(c->ev_converted[slot], c->stream));
+        }
     }
     c->n = n;
     c->sorted = 0;

@@ -71,9 +71,11 @@ struct pic_ctx {
     uint32_t* cellcount = nullptr;  // G+1
     picgb::ScanScratch scan;
 
-    // upload staging (device FP64)
+    // upload staging (device FP64, two slots) and its copy stream
     double* stage = nullptr;
     size_t stage_elems = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_converted[2] = {nullptr, nullptr};
 
     // grid
     long long* acc = nullptr;  // fixed-point rho accumulator (G)

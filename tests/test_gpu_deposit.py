@@ -254,3 +254,27 @@ def test_config2_full_size(port, pg, scheme):
     assert unit == wunit and np.array_equal(acc_s, want)
     rel = np.linalg.norm(rho - ref) / np.linalg.norm(ref)
     assert rel <= REL_L2_TOL, rel
+
+
+@pytest.mark.parametrize("grid", [(64, 48, 64.0, 48.0), (37, 23, 3.7, 2.3)])
+def test_pinned_upload_matches_pageable(port, pg, grid):
+    """Page-locked inputs are read by the conversion kernel over the host link;
+    the device layout must equal the staged (pageable) upload's bit for bit."""
+    nx, ny, lx, ly = grid
+    p = maxwellian(port, nx, ny, lx, ly, 300000, seed=17)
+    pins = {k: pg.PinnedArray(len(p["x"])) for k in ("x", "y", "vx", "vy", "q")}
+    try:
+        for k, a in pins.items():
+            a.array[:] = p[k]
+        with pg.Context(nx, ny, lx, ly, len(p["x"])) as c:
+            c.upload(pins["x"].array, pins["y"].array, pins["q"].array, pins["vx"].array, pins["vy"].array)
+            a = c.device_layout()
+            c.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"])
+            b = c.device_layout()
+        for k in a:
+            assert np.array_equal(a[k], b[k]), k
+        cell, xr, yr = port.to_device(nx, ny, lx, ly, p["x"], p["y"])
+        assert np.array_equal(a["cell"], cell) and np.array_equal(a["xr"], xr) and np.array_equal(a["yr"], yr)
+    finally:
+        for v in pins.values():
+            v.free()
