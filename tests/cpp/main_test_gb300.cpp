@@ -1,0 +1,338 @@
+// C++ checks of the pic:: host interface, written the way the reference's own
+// src/main_test.cpp is (expectNear, PASS/FAIL lines, exit status), against the
+// GB300 backend.
+//
+//   main_test_gb300                 run the checks (needs a GPU)
+//   main_test_gb300 init KIND OUT   write initialised particles (CPU only):
+//                                   KIND = maxwellian | langmuir | warm | twostream | quasi1d
+//   main_test_gb300 deposit S OUT   deposit 5000 particles on 128x128 with scheme S
+//                                   (NGP/CIC/TSC/Esirkepov), write particles + rho
+//
+// Output files are raw little-endian: u64 n, u64 Nx, u64 Ny, then x, y, vx, vy,
+// q, m (n doubles each) and, for "deposit", rho (Nx*Ny doubles).
+#include "pic_gb300_host.hpp"
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <iostream>
+#include <numeric>
+#include <string>
+
+namespace {
+
+bool expectNear(double value, double expected, double tol, const std::string& name) {
+    if (!(std::abs(value - expected) <= tol)) {
+        std::cerr << "FAIL " << name << ": got " << value << " expected " << expected << "\n";
+        return false;
+    }
+    std::cout << "PASS " << name << "\n";
+    return true;
+}
+
+double absCharge(const pic::ParticlesSoA& p) {
+    return std::accumulate(p.q().begin(), p.q().end(), 0.0, [](double s, double q) { return s + std::abs(q); });
+}
+
+// main_test.cpp:25-46
+bool testSchemeChargeConservation(pic::DepositionScheme scheme) {
+    pic::Domain domain;
+    domain.Nx = 32;
+    domain.Ny = 32;
+    domain.updateDerived();
+    pic::FieldGrid grid(domain);
+    pic::ParticlesSoA particles(1000);
+    particles.initializeUniformMaxwellian(domain, 1.0, 123);
+
+    pic::DepositionConfig cfg;
+    cfg.scheme = scheme;
+    cfg.esirkepov_dt = 0.0;
+    pic::depositChargeSoA(particles, grid, cfg);
+    const double err = pic::chargeConservationError(grid.integratedRho(), particles.totalCharge(), absCharge(particles));
+    return expectNear(err, 0.0, scheme == pic::DepositionScheme::NGP ? 0.05 : 1e-10,
+                      pic::schemeName(scheme) + " charge conservation");
+}
+
+// main_test.cpp:48-72
+bool testEsirkepovMovingChargeConservation() {
+    pic::Domain domain;
+    domain.Nx = 32;
+    domain.Ny = 32;
+    domain.updateDerived();
+    pic::FieldGrid grid(domain);
+    pic::ParticlesSoA particles(1000);
+    particles.initializeUniformMaxwellian(domain, 1.0, 123);
+
+    pic::DepositionConfig cfg;
+    cfg.scheme = pic::DepositionScheme::Esirkepov;
+    cfg.esirkepov_dt = 0.01;
+    pic::depositChargeSoA(particles, grid, cfg);
+    const double err = pic::chargeConservationError(grid.integratedRho(), particles.totalCharge(), absCharge(particles));
+    return expectNear(err, 0.0, 1e-10, "Esirkepov charge conservation (moving, dt=0.01)");
+}
+
+// main_test.cpp:74-87
+bool testWarmLangmuirFiniteEnergy() {
+    pic::Domain domain;
+    domain.Nx = 16;
+    domain.Ny = 16;
+    domain.updateDerived();
+    pic::ParticlesSoA particles(100);
+    particles.initializeWarmLangmuirWave(domain, 0.05, 1, 0.1, 42);
+    const double ke = particles.kineticEnergy();
+    if (!std::isfinite(ke) || ke <= 0.0) {
+        std::cerr << "FAIL warm Langmuir: non-finite or zero kinetic energy\n";
+        return false;
+    }
+    std::cout << "PASS warm Langmuir finite energy\n";
+    return true;
+}
+
+// main_test.cpp:158-180 (testGpuDeposit), on the GB300 backend
+bool testGpuDeposit() {
+    pic::Domain domain;
+    domain.Nx = 128;
+    domain.Ny = 128;
+    domain.updateDerived();
+    pic::FieldGrid grid(domain);
+    pic::ParticlesSoA particles(5000);
+    particles.initializeUniformMaxwellian(domain, 1.0, 123);
+
+    pic::DepositionConfig cfg;
+    cfg.scheme = pic::DepositionScheme::CIC;
+    cfg.backend = pic::DepositionBackend::GB300;
+    pic::depositChargeSoA(particles, grid, cfg);
+    const double err = pic::chargeConservationError(grid.integratedRho(), particles.totalCharge(), absCharge(particles));
+    return expectNear(err, 0.0, 1e-9, "GB300 CIC charge conservation");
+}
+
+bool testSortedDepositMatchesUnsorted() {
+    pic::Domain domain;
+    domain.Nx = 64;
+    domain.Ny = 64;
+    domain.updateDerived();
+    pic::ParticlesSoA particles(20000);
+    particles.initializeUniformMaxwellian(domain, 1.0, 7);
+    bool ok = true;
+    for (auto s : {pic::DepositionScheme::NGP, pic::DepositionScheme::CIC, pic::DepositionScheme::TSC}) {
+        pic::FieldGrid a(domain), b(domain);
+        pic::DepositionConfig cfg;
+        cfg.scheme = s;
+        pic::depositChargeSoA(particles, a, cfg);
+        cfg.sorted = true;
+        pic::depositChargeSoA(particles, b, cfg);
+        double diff = 0.0;
+        for (std::size_t i = 0; i < a.rho().size(); ++i) diff = std::max(diff, std::abs(a.rho()[i] - b.rho()[i]));
+        ok &= expectNear(diff, 0.0, 0.0, pic::schemeName(s) + " sorted == unsorted (bit-exact)");
+    }
+    return ok;
+}
+
+bool testSortByCell() {
+    pic::Domain domain;
+    domain.Nx = 48;
+    domain.Ny = 40;
+    domain.Lx = 3.0;
+    domain.Ly = 2.0;
+    domain.updateDerived();
+    pic::ParticlesSoA particles(10000);
+    particles.initializeUniformMaxwellian(domain, 1.0, 11);
+    const double q0 = particles.totalCharge();
+    pic::sortParticlesByCell(particles, domain);
+    int prev = -1;
+    bool ordered = true;
+    for (std::size_t i = 0; i < particles.size(); ++i) {
+        const int c = pic::particleCellIndex(particles.x()[i], particles.y()[i], domain);
+        ordered &= c >= prev;
+        prev = c;
+    }
+    bool ok = expectNear(ordered ? 0.0 : 1.0, 0.0, 0.0, "sortParticlesByCell cell order");
+    ok &= expectNear(particles.totalCharge(), q0, 0.0, "sortParticlesByCell keeps the charges");
+    return ok;
+}
+
+bool testTimedDeposit() {
+    pic::Domain domain;
+    domain.Nx = 256;
+    domain.Ny = 256;
+    domain.Lx = 256.0;
+    domain.Ly = 256.0;
+    domain.updateDerived();
+    pic::FieldGrid grid(domain);
+    pic::ParticlesSoA particles(1 << 20);
+    particles.initializeUniformMaxwellian(domain, 1.0, 42);
+    pic::DepositionConfig cfg;
+    cfg.scheme = pic::DepositionScheme::CIC;
+    cfg.sorted = true;
+    const auto st = pic::depositChargeTimedSoA(particles, grid, cfg, 5);
+    std::cout << "INFO timed CIC 256^2 1M: deposit " << st.deposit_ms << " ms, sort " << st.sort_ms << " ms, "
+              << st.throughput_particles_per_s << " particles/s\n";
+    bool ok = expectNear(st.charge_error, 0.0, 1e-10, "depositChargeTimedSoA charge error");
+    ok &= expectNear(st.throughput_particles_per_s > 0.0 ? 0.0 : 1.0, 0.0, 0.0, "depositChargeTimedSoA throughput");
+    return ok;
+}
+
+bool testPoissonAndMotion() {
+    pic::Domain domain;
+    domain.Nx = 64;
+    domain.Ny = 32;
+    domain.Lx = 2.0;
+    domain.Ly = 1.0;
+    domain.updateDerived();
+    pic::FieldGrid grid(domain);
+    pic::ParticlesSoA particles(4000);
+    particles.initializeWarmLangmuirWave(domain, 0.05, 1, 0.01, 5);
+    pic::DepositionConfig cfg;
+    pic::depositChargeSoA(particles, grid, cfg);
+    for (double& v : grid.rho()) v += 1.0 / domain.domainVolume();
+    pic::PoissonSolverFFT fft(domain);
+    fft.solve(grid);
+    const double fe_fft = grid.fieldEnergy();
+    bool ok = expectNear(fe_fft > 0.0 ? 0.0 : 1.0, 0.0, 0.0, "FFT field energy positive");
+
+    // RBGS against FFT on a smooth density: the 5-point and spectral Laplacians
+    // differ by (k*dx)^2/12 per mode, 1.3% for the (kx, ky) = (pi, 4*pi) mode here.
+    pic::FieldGrid sa(domain), sb(domain);
+    for (int iy = 0; iy < domain.Ny; ++iy)
+        for (int ix = 0; ix < domain.Nx; ++ix)
+            sa.rho()[domain.cellIndex(ix, iy)] = std::cos(2.0 * M_PI * ix * domain.dx / domain.Lx) +
+                                                  0.5 * std::sin(2.0 * M_PI * 2.0 * iy * domain.dy / domain.Ly);
+    sb.rho() = sa.rho();
+    fft.solve(sa);
+    pic::PoissonSolverGS gs(domain, 20000, 1e-10);
+    gs.solve(sb);
+    double dphi = 0.0, pmax = 0.0;
+    for (std::size_t i = 0; i < sa.phi().size(); ++i) {
+        dphi = std::max(dphi, std::abs(sa.phi()[i] - sb.phi()[i]));
+        pmax = std::max(pmax, std::abs(sa.phi()[i]));
+    }
+    std::cout << "INFO RBGS iterations " << gs.lastIterations() << "\n";
+    ok &= expectNear(dphi / pmax, 0.0, 2e-2, "RBGS phi agrees with FFT phi");
+
+    const double ke0 = particles.kineticEnergy();
+    pic::gatherFieldsSoA(particles, grid, 0.01);
+    pic::pushParticlesSoA(particles, grid, 0.01);
+    const double ke1 = particles.kineticEnergy();
+    ok &= expectNear((ke1 - ke0) / ke0, 0.0, 0.5, "gather + push keep the kinetic energy bounded");
+    for (std::size_t i = 0; i < particles.size(); ++i) {
+        if (!(particles.x()[i] >= 0.0 && particles.x()[i] < domain.Lx && particles.y()[i] >= 0.0 &&
+              particles.y()[i] < domain.Ly)) {
+            std::cerr << "FAIL push: particle " << i << " left the domain\n";
+            return false;
+        }
+    }
+    std::cout << "PASS push keeps particles in the periodic domain\n";
+    return ok;
+}
+
+bool testLangmuirSimulation() {
+    bool ok = true;
+    for (auto s : {pic::DepositionScheme::CIC, pic::DepositionScheme::TSC, pic::DepositionScheme::Esirkepov}) {
+        pic::SimulationConfig cfg;
+        cfg.domain.Nx = 64;
+        cfg.domain.Ny = 64;
+        cfg.domain.dt = 0.01;
+        cfg.domain.steps = 200;
+        cfg.domain.updateDerived();
+        cfg.num_particles = 20000;
+        cfg.scheme = s;
+        cfg.langmuir_mode = true;
+        cfg.sorted = true;
+        cfg.sort_interval = 5;
+        pic::Simulation sim(cfg);
+        const auto r = sim.run();
+        ok &= expectNear(r.final_charge_error, 0.0, 1e-10, "Simulation " + pic::schemeName(s) + " charge error");
+        ok &= expectNear(std::isfinite(r.energy_drift) ? 0.0 : 1.0, 0.0, 0.0,
+                         "Simulation " + pic::schemeName(s) + " finite energy");
+        ok &= expectNear(r.energy_history.size(), 200.0, 0.0, "Simulation " + pic::schemeName(s) + " history length");
+    }
+    return ok;
+}
+
+bool testUnsupportedBackendThrows() {
+    pic::Domain domain;
+    domain.updateDerived();
+    pic::FieldGrid grid(domain);
+    pic::ParticlesSoA particles(10);
+    particles.initializeUniformMaxwellian(domain, 1.0, 1);
+    pic::DepositionConfig cfg;
+    cfg.backend = pic::DepositionBackend::CPU;
+    try {
+        pic::depositChargeSoA(particles, grid, cfg);
+    } catch (const std::runtime_error&) {
+        std::cout << "PASS non-GB300 backend throws std::runtime_error\n";
+        return true;
+    }
+    std::cerr << "FAIL non-GB300 backend did not throw\n";
+    return false;
+}
+
+void writeParticles(std::FILE* f, const pic::ParticlesSoA& p, const pic::Domain& d) {
+    const uint64_t hdr[3] = {p.size(), static_cast<uint64_t>(d.Nx), static_cast<uint64_t>(d.Ny)};
+    std::fwrite(hdr, sizeof(uint64_t), 3, f);
+    for (const auto* v : {&p.x(), &p.y(), &p.vx(), &p.vy(), &p.q(), &p.m()})
+        std::fwrite(v->data(), sizeof(double), v->size(), f);
+}
+
+int dumpInit(const std::string& kind, const std::string& out) {
+    pic::Domain d;
+    d.Nx = 32;
+    d.Ny = 24;
+    d.Lx = 2.0;
+    d.Ly = 1.5;
+    d.updateDerived();
+    pic::ParticlesSoA p(2001);
+    if (kind == "maxwellian") p.initializeUniformMaxwellian(d, 0.7, 42);
+    else if (kind == "langmuir") p.initializeLangmuirWave(d, 0.01, 2, 42);
+    else if (kind == "warm") p.initializeWarmLangmuirWave(d, 0.05, 1, 0.1, 42);
+    else if (kind == "twostream") p.initializeTwoStream(d, 0.3, 0.01, 42);
+    else if (kind == "quasi1d") p.initializeTwoStreamQuasi1D(d, 0.3, 0.01, 42);
+    else return 2;
+    std::FILE* f = std::fopen(out.c_str(), "wb");
+    if (!f) return 3;
+    writeParticles(f, p, d);
+    std::fclose(f);
+    return 0;
+}
+
+int dumpDeposit(const std::string& scheme, const std::string& out) {
+    pic::Domain d;
+    d.Nx = 128;
+    d.Ny = 128;
+    d.updateDerived();
+    pic::FieldGrid grid(d);
+    pic::ParticlesSoA p(5000);
+    p.initializeUniformMaxwellian(d, 1.0, 123);
+    pic::DepositionConfig cfg;
+    cfg.scheme = pic::schemeFromString(scheme);
+    cfg.esirkepov_dt = cfg.scheme == pic::DepositionScheme::Esirkepov ? 0.001 : 0.0;
+    pic::depositChargeSoA(p, grid, cfg);
+    std::FILE* f = std::fopen(out.c_str(), "wb");
+    if (!f) return 3;
+    writeParticles(f, p, d);
+    std::fwrite(grid.rho().data(), sizeof(double), grid.rho().size(), f);
+    std::fclose(f);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc == 4 && std::string(argv[1]) == "init") return dumpInit(argv[2], argv[3]);
+    if (argc == 4 && std::string(argv[1]) == "deposit") return dumpDeposit(argv[2], argv[3]);
+    bool ok = true;
+    ok &= testSchemeChargeConservation(pic::DepositionScheme::CIC);
+    ok &= testSchemeChargeConservation(pic::DepositionScheme::TSC);
+    ok &= testSchemeChargeConservation(pic::DepositionScheme::Esirkepov);
+    ok &= testEsirkepovMovingChargeConservation();
+    ok &= testWarmLangmuirFiniteEnergy();
+    ok &= testSchemeChargeConservation(pic::DepositionScheme::NGP);
+    ok &= testGpuDeposit();
+    ok &= testSortedDepositMatchesUnsorted();
+    ok &= testSortByCell();
+    ok &= testTimedDeposit();
+    ok &= testPoissonAndMotion();
+    ok &= testLangmuirSimulation();
+    ok &= testUnsupportedBackendThrows();
+    return ok ? 0 : 1;
+}
