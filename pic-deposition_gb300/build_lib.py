@@ -76,7 +76,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     if host_srcs:
         host_hdrs = sorted(glob.glob(os.path.join(HOST, "**", "*.hpp"), recursive=True))
         if _stale(HOSTLIB, host_srcs + host_hdrs + [LIB]):
-            _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + INCLUDE, "-I" + HOST, "-o", HOSTLIB]
+            _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I" + INCLUDE, "-I" + HOST, "-o", HOSTLIB]
                  + host_srcs + ["-L" + LIBDIR, "-lpicgb300", "-Wl,-rpath,$ORIGIN"])
     if verbose or ptxas_info:
         sys.stdout.write("".join(logs))

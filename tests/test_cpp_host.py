@@ -32,7 +32,7 @@ def exe():
     build_lib.build()
     hdr = os.path.join(PKG, "host", "pic_gb300_host.hpp")
     if build_lib._stale(EXE, [SRC, hdr, build_lib.HOSTLIB]):
-        subprocess.run(["g++", "-O2", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"),
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"),
                         "-I" + os.path.join(PKG, "host"), SRC, "-o", EXE, "-L" + LIBDIR, "-lpicgb300_host",
                         "-lpicgb300", "-Wl,-rpath," + LIBDIR], check=True)
     return EXE
