@@ -242,6 +242,71 @@ int pic_gpu_deposit_noalloc(const pic_domain* domain, int scheme, const uint32_t
                             const float* yr, const float* qn, size_t n, float max_abs_q, double background,
                             double* rho, void* stream);
 
+/* ---- learned warm start for the red-black Gauss-Seidel solve ----
+ *
+ * No counterpart in the reference (its PoissonSolverGS, src/pic/poisson_gs.cpp:11-61,
+ * starts from zero every call). Three starting guesses for the same solve, each
+ * iterated to the same relative residual:
+ *   0  the previous step's phi (the plain method and the fallback),
+ *   1  the cubic extrapolation E = 3 phi[n-1] - 3 phi[n-2] + phi[n-3],
+ *   2  E + s * sigma * net(r / sigma), r = b - A E, sigma = rms(r): a 6-layer 3x3
+ *      convolutional network (32 channels, BF16 on the tensor cores, FP32
+ *      accumulation) trained on the run's own converged solutions.
+ * Needs Nx a multiple of 128 and even Ny. Parameters: one FP32 array, per layer
+ * w[9][cout][cin] then bias[cout], channels (16,32),(32,32)x4,(32,16) of which
+ * the first layer's input and the last layer's output use channel 0 only. */
+typedef struct pic_ws_stats {
+    int iters[3];          /* sweeps from guesses 0, 1, 2 */
+    double ms[3];          /* device time of each solve: guess + sweeps + checks */
+    double resid[3];       /* final relative residual */
+    double guess_resid[3]; /* relative residual of the guess itself */
+    double phi_diff;       /* rms difference of the guess-2 solution from the guess-0 one */
+} pic_ws_stats;
+
+size_t pic_gpu_ws_param_count(void);
+/* Creates the network (He-normal initialisation from `seed`) and a device
+ * dataset of up to `dataset_capacity` (input, target) pairs of Nx*Ny BF16 each. */
+int pic_gpu_ws_init(pic_ctx* ctx, unsigned seed, size_t dataset_capacity);
+int pic_gpu_ws_get_params(pic_ctx* ctx, float* params, size_t n);
+int pic_gpu_ws_set_params(pic_ctx* ctx, const float* params, size_t n);
+/* Advances the resident particles `steps` steps (gather+push, cell sort every
+ * sort_interval steps, CIC deposit + background, exact solve of the 5-point
+ * system) and appends one training pair per step once three solutions exist. */
+int pic_gpu_ws_generate(pic_ctx* ctx, int steps, double dt, double background, int sort_interval);
+int pic_gpu_ws_dataset_size(pic_ctx* ctx, size_t* n);
+/* Adam (beta 0.9, 0.999) on the mean squared error over shuffled batches;
+ * loss_per_epoch[epochs] (may be NULL) gets each epoch's mean loss. */
+int pic_gpu_ws_train(pic_ctx* ctx, int epochs, int batch, float lr, unsigned seed, double* loss_per_epoch);
+/* Loss and gradient of one batch (inputs, targets: batch*Nx*Ny floats, rounded to
+ * BF16 on the device), for checking the backward pass. */
+int pic_gpu_ws_loss_grad(pic_ctx* ctx, int batch, const float* inputs, const float* targets, double* loss,
+                         float* grad);
+/* Network output (Nx*Ny floats) for one input field. */
+int pic_gpu_ws_predict(pic_ctx* ctx, const float* input, float* output);
+/* Advances `steps` steps as pic_gpu_ws_generate does, but solves each step's
+ * system by red-black Gauss-Seidel three times, from guesses 0, 1 and 2, to
+ * `tol` (checked every check_every sweeps, at most max_iters), timing each on
+ * the device; the run continues with the guess-0 solution. */
+int pic_gpu_ws_study(pic_ctx* ctx, int steps, double dt, double background, int sort_interval, double tol,
+                     int check_every, int max_iters, pic_ws_stats* stats);
+
+/* ---- 3x3 periodic convolution layers on the tensor cores (BF16, FP32 accumulate) ----
+ *
+ * No counterpart in the reference: the layers of the learned warm start for the
+ * red-black Gauss-Seidel solve. This entry runs one layer on host buffers, on
+ * the current device, synchronously (it allocates and frees device memory).
+ * Tensors are NHWC with BF16 bit patterns; weights FP32 w[tap][cout][cin] with
+ * tap = (dy+1)*3 + (dx+1), rounded to BF16 on the device. W must be a multiple
+ * of 128 (op 3: of 64); cin, cout in {16, 32}.
+ *   op 0: out(BF16, cout ch) = relu(conv(x) + bias)            x: cin channels
+ *   op 1: out(FP32, 1 ch)    = conv(x)[channel 0] + bias[0]     x: cin channels
+ *   op 2: out(BF16, cin ch)  = conv^T(x) * (aux > 0)            x: cout channels (the
+ *         output gradient), aux: cin channels (the layer input, its ReLU mask)
+ *   op 3: out(FP32)          = dL/dw [9][cout][cin] then dL/dbias [cout],
+ *         x: the layer input (cin ch), aux: the output gradient (cout ch) */
+int pic_nn_conv3x3(int op, int batch, int H, int W, int cin, int cout, const uint16_t* x, const float* weight,
+                   const float* bias, const uint16_t* aux, void* out);
+
 #ifdef __cplusplus
 }
 #endif

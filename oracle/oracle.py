@@ -94,6 +94,62 @@ class Port:
         L.orc_move_f32.argtypes = [D, C.c_size_t, _u32p, _fp, _fp, _fp, _fp, _fp, C.c_float, C.c_void_p, _dp, _dp,
                                    C.c_double, C.c_int, C.c_int]
 
+        _u16p = np.ctypeslib.ndpointer(dtype=np.uint16, flags="C_CONTIGUOUS")
+        L.orc_conv3x3_fwd.argtypes = [C.c_int] * 5 + [_u16p, _fp, _fp, C.c_int, C.c_void_p]
+        L.orc_conv3x3_dgrad.argtypes = [C.c_int] * 5 + [_u16p, _fp, _u16p, _u16p]
+        L.orc_conv3x3_wgrad.argtypes = [C.c_int] * 5 + [_u16p, _u16p, _dp, _dp]
+        L.orc_net_param_count.restype = C.c_size_t
+        L.orc_net_loss_grad.argtypes = [C.c_int] * 3 + [_fp, _fp, _fp, C.c_int, C.POINTER(C.c_double), _dp]
+        L.orc_bf16_from_float.argtypes = [C.c_float]
+        L.orc_bf16_from_float.restype = C.c_uint16
+
+    # ---- the warm-start network (nn_oracle.c) ----
+    @staticmethod
+    def bf16(a):
+        """Float array -> BF16 bit patterns (round to nearest even)."""
+        u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+        r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+        return r
+
+    @staticmethod
+    def from_bf16(h):
+        return (np.ascontiguousarray(h, dtype=np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+    def conv_fwd(self, x, w, bias, relu=True):
+        B, H, W, cin = x.shape
+        cout = w.shape[1]
+        out = np.zeros((B, H, W, cout), np.uint16) if relu else np.zeros((B, H, W), np.float32)
+        self.lib.orc_conv3x3_fwd(B, H, W, cin, cout, _c(x, np.uint16), _c(w, np.float32), _c(bias, np.float32),
+                                 0 if relu else 1, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def conv_dgrad(self, dy, w, mask):
+        B, H, W, cout = dy.shape
+        cin = w.shape[2]
+        out = np.zeros((B, H, W, cin), np.uint16)
+        self.lib.orc_conv3x3_dgrad(B, H, W, cin, cout, _c(dy, np.uint16), _c(w, np.float32), _c(mask, np.uint16),
+                                   out)
+        return out
+
+    def conv_wgrad(self, x, dy):
+        B, H, W, cin = x.shape
+        cout = dy.shape[3]
+        dw = np.zeros(9 * cout * cin)
+        db = np.zeros(cout)
+        self.lib.orc_conv3x3_wgrad(B, H, W, cin, cout, _c(x, np.uint16), _c(dy, np.uint16), dw, db)
+        return dw.reshape(9, cout, cin), db
+
+    def net_param_count(self):
+        return int(self.lib.orc_net_param_count())
+
+    def net_loss_grad(self, params, inp, target, quantize=True):
+        B, H, W = inp.shape
+        grad = np.zeros(self.net_param_count())
+        loss = C.c_double()
+        self.lib.orc_net_loss_grad(B, H, W, _c(params, np.float32), _c(inp, np.float32), _c(target, np.float32),
+                                   1 if quantize else 0, C.byref(loss), grad)
+        return loss.value, grad
+
     @staticmethod
     def dom(nx, ny, lx, ly):
         return C.byref(_Domain(float(lx), float(ly), int(nx), int(ny)))

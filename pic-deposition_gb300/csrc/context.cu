@@ -386,6 +386,7 @@ int pic_gpu_destroy(pic_ctx* c) {
     release_fields(c);
     release_rbgs(c);
     release_current(c);
+    release_ws(c);
     prof_clear(c, nullptr);
     delete c->prof;
     for (int k = 0; k < 2; ++k) {

@@ -269,6 +269,41 @@ int poisson_fft(pic_ctx* c) {
     return efield_from_phi(c);
 }
 
+// spectrum /= eigenvalue of the 5-point operator
+//   denom - 2*ix2*cos(2*pi*mx/Nx) - 2*iy2*cos(2*pi*my/Ny), DC = 0
+__global__ void k_divide_discrete(cufftDoubleComplex* __restrict__ spec, int Nx, int Ny, double ix2, double iy2,
+                                  double denom) {
+    const int nh = Nx / 2 + 1;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)nh * Ny) return;
+    const int i = (int)(t % nh), j = (int)(t / nh);
+    if (i == 0 && j == 0) {
+        spec[t].x = 0.0;
+        spec[t].y = 0.0;
+        return;
+    }
+    const double twopi = 2.0 * 3.14159265358979323846;
+    const double cx = cos(twopi * (double)i / (double)Nx), cy = cos(twopi * (double)j / (double)Ny);
+    const double lam = denom - 2.0 * ix2 * cx - 2.0 * iy2 * cy;
+    spec[t].x = spec[t].x / lam;
+    spec[t].y = spec[t].y / lam;
+}
+
+int solve_discrete_fft(pic_ctx* c, const double* b, double* phi) {
+    PIC_TRY(ensure_fft(c));
+    double ix2, iy2, denom;
+    rbgs_operator(c, &ix2, &iy2, &denom);
+    PIC_CUDA_TRY(cudaMemcpyAsync(c->fft_rhs, b, c->G * 8, cudaMemcpyDeviceToDevice, c->stream));
+    PIC_CUFFT_TRY(cufftExecD2Z((cufftHandle)c->fft_fwd, c->fft_rhs, (cufftDoubleComplex*)c->spec));
+    const size_t ns = (size_t)(c->Nx / 2 + 1) * c->Ny;
+    k_divide_discrete<<<(unsigned)((ns + 255) / 256), 256, 0, c->stream>>>((cufftDoubleComplex*)c->spec, c->Nx,
+                                                                            c->Ny, ix2, iy2, denom);
+    PIC_TRY(check_launch(c, "k_divide_discrete"));
+    PIC_CUFFT_TRY(cufftExecZ2D((cufftHandle)c->fft_inv, (cufftDoubleComplex*)c->spec, phi));
+    scale_phi<<<(unsigned)((c->G + 255) / 256), 256, 0, c->stream>>>(phi, c->G, 1.0 / (double)c->G);
+    return check_launch(c, "scale_phi");
+}
+
 // Queues the six diagnostics into c->red_out[0..5] (pic_diag order).
 int diagnostics_async(pic_ctx* c) {
     PIC_TRY(ensure_fields(c));

@@ -39,6 +39,8 @@ enum DevErr : int {
 // from a 4-aligned index below n, which may reach up to 3 elements past n.
 constexpr size_t PARTICLE_PAD = 32;
 
+struct WsState;
+
 struct ScanScratch {
     unsigned int* partials = nullptr;  // per-level block sums
     size_t capacity = 0;               // elements in partials
@@ -97,7 +99,9 @@ struct pic_ctx {
     // red-black Gauss-Seidel
     double *rb_b = nullptr, *rb_partial = nullptr, *rb_scalars = nullptr;
     int last_rbgs_iters = 0;
-    double last_rbgs_resid = 0.0;
+    double last_rbgs_resid = 0.0, first_rbgs_resid = 0.0;
+    // learned warm start (warmstart.cu)
+    picgb::WsState* ws = nullptr;
     // Esirkepov current: int64 edge grids, FP64 copies, units (x, y)
     long long *accjx = nullptr, *accjy = nullptr;
     double *jx = nullptr, *jy = nullptr, *junits = nullptr;
@@ -156,6 +160,19 @@ void release_rbgs(pic_ctx* ctx);
 void release_current(pic_ctx* ctx);
 // Deposit (deposit.cu).
 int deposit_rho(pic_ctx* ctx, int scheme, double dt, double background);
+// Red-black Gauss-Seidel pieces (rbgs.cu): right-hand side b = rho*dV - mean into
+// the solver's buffer; r = b - A phi; the 5-point operator's coefficients; a
+// solve from the phi in the context.
+int rbgs_prepare(pic_ctx* ctx);
+int rbgs_residual_field(pic_ctx* ctx, const double* phi, double* r);
+void rbgs_operator(pic_ctx* ctx, double* ix2, double* iy2, double* denom);
+int rbgs_solve(pic_ctx* ctx, double tol, int max_iters, int check_every, int* iters_out, double* resid_out);
+// Exact solution of the 5-point system A phi = b (b with zero mean), by FFT with
+// the operator's own eigenvalues (fields.cu).
+int solve_discrete_fft(pic_ctx* ctx, const double* b, double* phi);
+// Particle motion (push.cu).
+int move(pic_ctx* ctx, double dt, bool gather, bool push);
+void release_ws(pic_ctx* ctx);
 
 // Brackets a kernel launch with profiling events when enabled.
 void prof_begin(pic_ctx* ctx, const char* name);

@@ -201,6 +201,7 @@ int rbgs_solve(pic_ctx* c, double tol, int max_iters, int check_every, int* iter
         PIC_CUDA_TRY(cudaMemcpyAsync(s, c->rb_scalars, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
         PIC_CUDA_TRY(cudaStreamSynchronize(c->stream));
         res = s[2] > 0.0 ? std::sqrt(s[1] / s[2]) : std::sqrt(s[1]);
+        if (it == 0) c->first_rbgs_resid = res;
         if (res <= tol || it >= max_iters) break;
         const int n = (max_iters - it) < check_every ? (max_iters - it) : check_every;
         PIC_TRY(rb_sweeps(c, a, n));
@@ -213,6 +214,38 @@ int rbgs_solve(pic_ctx* c, double tol, int max_iters, int check_every, int* iter
     c->last_rbgs_iters = it;
     c->last_rbgs_resid = res;
     return PIC_OK;
+}
+
+// r = b - A phi for the right-hand side prepared by rbgs_prepare.
+__global__ void rb_residual_field(RbArgs a, const double* __restrict__ phi, double* __restrict__ r) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (size_t)a.Nx * a.Ny) return;
+    const int j = (int)(id / a.Nx), i = (int)(id - (size_t)j * a.Nx);
+    const int im = i == 0 ? a.Nx - 1 : i - 1, ip = i == a.Nx - 1 ? 0 : i + 1;
+    const int jm = j == 0 ? a.Ny - 1 : j - 1, jp = j == a.Ny - 1 ? 0 : j + 1;
+    const double we = __dadd_rn(phi[(size_t)j * a.Nx + im], phi[(size_t)j * a.Nx + ip]);
+    const double sn = __dadd_rn(phi[(size_t)jm * a.Nx + i], phi[(size_t)jp * a.Nx + i]);
+    const double ap = __dsub_rn(__dsub_rn(__dmul_rn(a.denom, phi[id]), __dmul_rn(we, a.ix2)), __dmul_rn(sn, a.iy2));
+    r[id] = __dsub_rn(a.b[id], ap);
+}
+
+int rbgs_prepare(pic_ctx* c) {
+    if ((c->Nx & 1) || (c->Ny & 1)) return fail(PIC_ERR_UNSUPPORTED, "red-black Gauss-Seidel needs even Nx and Ny");
+    PIC_TRY(ensure_rbgs(c));
+    return rb_prepare(c);
+}
+
+int rbgs_residual_field(pic_ctx* c, const double* phi, double* r) {
+    const RbArgs a = rb_args(c);
+    rb_residual_field<<<(unsigned)((c->G + 255) / 256), 256, 0, c->stream>>>(a, phi, r);
+    return check_launch(c, "rb_residual_field");
+}
+
+void rbgs_operator(pic_ctx* c, double* ix2, double* iy2, double* denom) {
+    const RbArgs a = rb_args(c);
+    *ix2 = a.ix2;
+    *iy2 = a.iy2;
+    *denom = a.denom;
 }
 
 int rbgs_solve_async(pic_ctx* c, double tol, int max_iters, int check_every) {

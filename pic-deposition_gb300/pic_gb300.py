@@ -98,6 +98,57 @@ class RunConfig(C.Structure):
 _SIGS.append(("pic_gpu_run", [_vp, C.POINTER(RunConfig), C.c_int, C.POINTER(_Diag)]))
 _SIGS.append(("pic_gpu_deposit_current", [_vp, C.c_double, _vp, _vp]))
 _SIGS.append(("pic_gpu_get_current_fixed", [_vp, _vp, _vp, _dp, _dp]))
+_SIGS.append(("pic_nn_conv3x3", [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]))
+
+NN_FWD_RELU, NN_FWD_OUT, NN_DGRAD, NN_WGRAD = 0, 1, 2, 3
+
+
+class WsStats(C.Structure):
+    """pic_ws_stats (include/pic_gb300.h): one step of the warm-start study."""
+    _fields_ = [("iters", C.c_int * 3), ("ms", C.c_double * 3), ("resid", C.c_double * 3),
+                ("guess_resid", C.c_double * 3), ("phi_diff", C.c_double)]
+
+
+_fp = C.POINTER(C.c_float)
+_SIGS += [
+    ("pic_gpu_ws_init", [_vp, C.c_uint, C.c_size_t]),
+    ("pic_gpu_ws_get_params", [_vp, _vp, C.c_size_t]),
+    ("pic_gpu_ws_set_params", [_vp, _vp, C.c_size_t]),
+    ("pic_gpu_ws_generate", [_vp, C.c_int, C.c_double, C.c_double, C.c_int]),
+    ("pic_gpu_ws_dataset_size", [_vp, C.POINTER(C.c_size_t)]),
+    ("pic_gpu_ws_train", [_vp, C.c_int, C.c_int, C.c_float, C.c_uint, _vp]),
+    ("pic_gpu_ws_loss_grad", [_vp, C.c_int, _vp, _vp, _dp, _vp]),
+    ("pic_gpu_ws_predict", [_vp, _vp, _vp]),
+    ("pic_gpu_ws_study", [_vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int, C.c_int,
+                          C.POINTER(WsStats)]),
+]
+
+
+def nn_conv3x3(op: int, x: np.ndarray, weight=None, bias=None, aux=None, cin: int = 32, cout: int = 32):
+    """One tensor-core convolution layer on host arrays (pic_nn_conv3x3).
+
+    x and aux are uint16 BF16 bit patterns shaped (B, H, W, C); weight is FP32
+    (9, cout, cin), bias FP32 (cout,). Returns BF16 bits (B, H, W, C) for ops 0
+    and 2, FP32 (B, H, W) for op 1 and (dw (9, cout, cin), db (cout,)) for op 3.
+    """
+    B, H, W = x.shape[:3]
+    x = np.ascontiguousarray(x, dtype=np.uint16)
+    ptr = lambda a: None if a is None else a.ctypes.data_as(_vp)
+    w = None if weight is None else np.ascontiguousarray(weight, dtype=np.float32)
+    b = None if bias is None else np.ascontiguousarray(bias, dtype=np.float32)
+    a = None if aux is None else np.ascontiguousarray(aux, dtype=np.uint16)
+    if op == NN_FWD_RELU:
+        out = np.zeros((B, H, W, cout), np.uint16)
+    elif op == NN_FWD_OUT:
+        out = np.zeros((B, H, W), np.float32)
+    elif op == NN_DGRAD:
+        out = np.zeros((B, H, W, cin), np.uint16)
+    else:
+        out = np.zeros(9 * cout * cin + cout, np.float32)
+    _check(lib().pic_nn_conv3x3(op, B, H, W, cin, cout, ptr(x), ptr(w), ptr(b), ptr(a), ptr(out)))
+    if op == NN_WGRAD:
+        return out[:9 * cout * cin].reshape(9, cout, cin), out[9 * cout * cin:]
+    return out
 
 
 class PinnedArray:
@@ -302,6 +353,62 @@ class Context:
         _check(lib().pic_gpu_poisson_rbgs(self.h, float(tol), int(max_iters), int(warm_start), int(check_every),
                                           C.byref(it), C.byref(res)))
         return it.value, res.value
+
+    # ---- learned warm start (pic_gpu_ws_*) ----
+    def ws_init(self, seed: int = 1, dataset_capacity: int = 0):
+        _check(lib().pic_gpu_ws_init(self.h, int(seed), int(dataset_capacity)))
+
+    @staticmethod
+    def ws_param_count() -> int:
+        L = lib()
+        L.pic_gpu_ws_param_count.restype = C.c_size_t
+        return int(L.pic_gpu_ws_param_count())
+
+    def ws_params(self) -> np.ndarray:
+        p = np.zeros(self.ws_param_count(), np.float32)
+        _check(lib().pic_gpu_ws_get_params(self.h, _ptr(p), p.size))
+        return p
+
+    def ws_set_params(self, p):
+        p = _arr(p, np.float32)
+        _check(lib().pic_gpu_ws_set_params(self.h, _ptr(p), p.size))
+
+    def ws_generate(self, steps, dt, background=0.0, sort_interval=20) -> int:
+        _check(lib().pic_gpu_ws_generate(self.h, int(steps), float(dt), float(background), int(sort_interval)))
+        n = C.c_size_t()
+        _check(lib().pic_gpu_ws_dataset_size(self.h, C.byref(n)))
+        return n.value
+
+    def ws_train(self, epochs, batch, lr=1e-3, seed=1) -> np.ndarray:
+        loss = np.zeros(max(int(epochs), 1))
+        _check(lib().pic_gpu_ws_train(self.h, int(epochs), int(batch), float(lr), int(seed), _ptr(loss)))
+        return loss[:epochs]
+
+    def ws_loss_grad(self, inputs, targets):
+        inputs = _arr(inputs, np.float32)
+        targets = _arr(targets, np.float32)
+        grad = np.zeros(self.ws_param_count(), np.float32)
+        loss = C.c_double()
+        _check(lib().pic_gpu_ws_loss_grad(self.h, inputs.shape[0], _ptr(inputs), _ptr(targets), C.byref(loss),
+                                          _ptr(grad)))
+        return loss.value, grad
+
+    def ws_predict(self, field):
+        field = _arr(field, np.float32)
+        out = np.zeros(field.size, np.float32)
+        _check(lib().pic_gpu_ws_predict(self.h, _ptr(field), _ptr(out)))
+        return out.reshape(field.shape)
+
+    def ws_study(self, steps, dt, background=0.0, sort_interval=20, tol=1e-8, check_every=16,
+                 max_iters=2_000_000) -> dict:
+        st = (WsStats * max(int(steps), 1))()
+        _check(lib().pic_gpu_ws_study(self.h, int(steps), float(dt), float(background), int(sort_interval), float(tol),
+                                      int(check_every), int(max_iters), st))
+        st = st[:steps]
+        return {"iters": np.array([list(s.iters) for s in st]), "ms": np.array([list(s.ms) for s in st]),
+                "resid": np.array([list(s.resid) for s in st]),
+                "guess_resid": np.array([list(s.guess_resid) for s in st]),
+                "phi_diff": np.array([s.phi_diff for s in st])}
 
     def run(self, steps, scheme=1, dt=0.01, background=0.0, sort_interval=0, use_graph=False, poisson=0,
             rbgs_tol=1e-8, rbgs_max_iters=100000, rbgs_check_every=64):
