@@ -50,6 +50,15 @@ SCHEMES = {"NGP": 0, "CIC": 1, "TSC": 2, "Esirkepov": 3}
 BYTES_PER_PARTICLE = 16  # x_rel, y_rel, q (FP32) + cell key (u32)
 BYTES_PER_PARTICLE_ESK = 24  # + vx, vy
 BYTES_PER_CELL = 8  # int64 rho written once
+# learned warm start for red-black Gauss-Seidel: 512x512, 64 particles per cell,
+# density 1 + 0.05*cos(2*pi*x/512), vth = 1 (the reference's charge convention,
+# total charge -1 and m = 1, with the neutralising background), dt = 0.1
+GS_N = 512
+GS_PPC = 64
+GS_AMP = 0.05
+GS_VTH = 1.0
+GS_DT = 0.1
+GS_TOL = 1e-8
 METRIC = "deposit particles/s (CIC, 64M cell-sorted particles, 1024x1024)"
 WORKLOAD = "cic_deposit_1024x1024_64ppc_sorted"
 
@@ -471,6 +480,83 @@ def run_gpu(args, d: Dist):
     }
 
 
+def ensemble_members(seed=4, runs=64):
+    """64 Langmuir runs: grid N from {128, 256, 512, 1024} and particles per cell
+    from {4, 16, 64, 256}, drawn per run from `seed`."""
+    rng = np.random.default_rng(seed)
+    ns = rng.choice([128, 256, 512, 1024], runs)
+    ppcs = rng.choice([4, 16, 64, 256], runs)
+    return [(int(n), int(p), int(1000 + i)) for i, (n, p) in enumerate(zip(ns, ppcs))]
+
+
+def run_ensemble(args):
+    """Batched ensemble: every run's step (gather+push, deposit, FFT Poisson) in one
+    persistent launch + batched FFTs per step, replayed as a CUDA graph."""
+    import pic_gb300 as pg
+
+    members = ensemble_members(runs=args.ens_runs)
+    total = sum(n * n * p for n, p, _ in members)
+    out = {"workload": f"ensemble_{len(members)}_langmuir_runs", "runs": len(members), "particles": total,
+           "cells": sum(n * n for n, _, _ in members), "dt": 0.1, "amplitude": 0.01, "vth": 0.05,
+           "sort_interval": args.ens_sort, "steps": args.ens_steps}
+    with pg.Ensemble(members, dt=0.1, amplitude=0.01, vth=0.05, sort_interval=args.ens_sort, use_graph=True) as e:
+        e.run(args.ens_sort + 1)  # warm-up: first sort, autotuning, graph capture
+        stream = e.stream()
+        ev = CudaEvents()
+        e0, e1 = ev.event(), ev.event()
+        l0 = e.launch_count()
+        ev.record(e0, stream)
+        fe, ke = e.run(args.ens_steps)
+        ev.record(e1, stream)
+        ms = ev.elapsed_ms(e0, e1)
+        out["launches_per_step"] = (e.launch_count() - l0) / args.ens_steps
+        out["tiles"] = sorted({f"N{e.info(r)['N']}_ppc{e.info(r)['ppc']}": list(e.info(r)["tile"])
+                               for r in range(len(members))}.items())
+    out["ms_per_step"] = ms / args.ens_steps
+    out["particle_steps_per_s"] = total * args.ens_steps / (ms * 1e-3)
+    out["field_energy_finite"] = bool(np.all(np.isfinite(fe)))
+    return out
+
+
+def run_gs_study(args):
+    """Time to a 1e-8 relative residual of red-black Gauss-Seidel from three
+    starting guesses (previous phi; cubic extrapolation; extrapolation plus the
+    trained network), each step's system solved three times from the same b."""
+    import pic_gb300 as pg
+    import workloads
+
+    p = workloads.density_cos(GS_N, GS_N, GS_PPC, GS_AMP, GS_VTH, seed=7)
+    n = len(p["x"])
+    p["q"] = np.full(n, -1.0 / n)
+    bg = 1.0 / (GS_N * GS_N)
+    out = {"workload": f"rbgs_{GS_N}x{GS_N}_{GS_PPC}ppc_landau", "particles": n, "tol": GS_TOL, "dt": GS_DT,
+           "pairs_requested": args.gs_pairs}
+    with pg.Context(GS_N, GS_N, float(GS_N), float(GS_N), n) as c:
+        c.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"])
+        del p
+        c.ws_init(seed=1, dataset_capacity=args.gs_pairs)
+        t0 = time.time()
+        out["pairs"] = c.ws_generate(args.gs_pairs + 3, GS_DT, bg, sort_interval=20)
+        out["generate_s"] = time.time() - t0
+        t0 = time.time()
+        losses = c.ws_train(args.gs_epochs, args.gs_batch, args.gs_lr)
+        out["train_s"] = time.time() - t0
+        out["train_loss"] = [float(v) for v in losses]
+        out["epochs"], out["batch"], out["lr"] = args.gs_epochs, args.gs_batch, args.gs_lr
+        st = c.ws_study(args.gs_steps, GS_DT, bg, sort_interval=20, tol=GS_TOL, check_every=args.gs_check)
+    names = ["previous_phi", "extrapolated", "extrapolated_plus_net"]
+    out["check_every"] = args.gs_check
+    out["steps"] = args.gs_steps
+    for k, nm in enumerate(names):
+        out[nm] = {"sweeps_mean": float(st["iters"][:, k].mean()), "ms_mean": float(st["ms"][:, k].mean()),
+                   "guess_resid_mean": float(st["guess_resid"][:, k].mean()),
+                   "resid_max": float(st["resid"][:, k].max())}
+    out["speedup_learned_vs_plain"] = out[names[0]]["ms_mean"] / out[names[2]]["ms_mean"]
+    out["speedup_extrapolated_vs_plain"] = out[names[0]]["ms_mean"] / out[names[1]]["ms_mean"]
+    out["phi_diff_max"] = float(st["phi_diff"].max())
+    return out
+
+
 def main():
     global PPC
     ap = argparse.ArgumentParser()
@@ -483,10 +569,29 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ppc", type=int, default=PPC, help="particles per cell (64 = the benchmark workload)")
     ap.add_argument("--deposit-only", action="store_true", help="reduced run for profilers")
+    ap.add_argument("--gs-only", action="store_true", help="only the Gauss-Seidel warm-start study")
+    ap.add_argument("--no-gs", action="store_true", help="skip the Gauss-Seidel warm-start study")
+    ap.add_argument("--ens-only", action="store_true", help="only the batched ensemble")
+    ap.add_argument("--no-ens", action="store_true", help="skip the batched ensemble")
+    ap.add_argument("--ens-runs", type=int, default=64)
+    ap.add_argument("--ens-steps", type=int, default=500)
+    ap.add_argument("--ens-sort", type=int, default=20)
+    ap.add_argument("--gs-pairs", type=int, default=20000)
+    ap.add_argument("--gs-epochs", type=int, default=2)
+    ap.add_argument("--gs-batch", type=int, default=16)
+    ap.add_argument("--gs-lr", type=float, default=1e-3)
+    ap.add_argument("--gs-steps", type=int, default=8)
+    ap.add_argument("--gs-check", type=int, default=16)
     args = ap.parse_args()
     PPC = args.ppc
     if args.warmup < 3:
         args.warmup = 3
+    if args.gs_only:
+        print(json.dumps(run_gs_study(args)), flush=True)
+        return
+    if args.ens_only:
+        print(json.dumps(run_ensemble(args)), flush=True)
+        return
     d = Dist()
     if args.deposit_only:
         run_deposit_only(args, d)
@@ -494,6 +599,11 @@ def main():
         return
     try:
         res = run_reference(args, d) if args.impl == "reference" else run_gpu(args, d)
+        if res is not None and args.impl != "reference" and d.ws == 1:
+            if not args.no_ens:
+                res["ensemble"] = run_ensemble(args)
+            if not args.no_gs:
+                res["gs_warm_start"] = run_gs_study(args)
     finally:
         d.close()
     if res is not None:

@@ -290,6 +290,55 @@ int pic_gpu_ws_predict(pic_ctx* ctx, const float* input, float* output);
 int pic_gpu_ws_study(pic_ctx* ctx, int steps, double dt, double background, int sort_interval, double tol,
                      int check_every, int max_iters, pic_ws_stats* stats);
 
+/* ---- batched ensemble of independent runs ----
+ *
+ * No counterpart in the reference (it runs one Simulation at a time,
+ * src/pic/simulation.cpp:69-145). Many Langmuir-oscillation runs with uneven
+ * grids (N x N cells, dx = dy = 1) and particle counts advance together: per
+ * step every run does gather + push, [cell sort every sort_interval steps], CIC
+ * deposit in fixed point + background 1, FFT Poisson (continuous k^2, as
+ * PoissonSolverFFT) and E, with the particle work of a step in one persistent
+ * cooperative launch and, with use_graph, the whole step one CUDA graph.
+ * Particles are generated on the device (counter-based random numbers, seed per
+ * run): x from the density 1 + amplitude*cos(2*pi*x/N), y uniform, Maxwellian v
+ * of thermal speed vth; charge -1/ppc and mass 1/ppc per particle (mean charge
+ * density -1, omega_p = 1). Each run's state equals that of the same run
+ * advanced alone through pic_gpu_run (scheme CIC, FFT Poisson, background 1). */
+typedef struct pic_ens pic_ens;
+typedef struct pic_ens_member {
+    int N;          /* grid N x N (even) */
+    int ppc;        /* particles per cell */
+    unsigned seed;  /* per-run seed (mixed with pic_ens_config.seed) */
+} pic_ens_member;
+typedef struct pic_ens_config {
+    double dt;
+    double amplitude;   /* density perturbation on mode 1 */
+    double vth;         /* thermal speed per component */
+    int sort_interval;  /* cell sort every this many steps (0 = never) */
+    int use_graph;
+    unsigned seed;
+} pic_ens_config;
+typedef struct pic_ens_run_info {
+    int N, ppc;
+    size_t particles;
+    int tile_w, tile_h; /* deposit tile chosen by the autotuner (after the first sorted step) */
+} pic_ens_run_info;
+
+/* Runs are reordered by grid size (stable); pic_ens_info gives run r's setup in that order. */
+int pic_ens_create(const pic_ens_member* runs, int nruns, const pic_ens_config* cfg, int device, pic_ens** out);
+int pic_ens_destroy(pic_ens* ens);
+/* Advances every run `steps` steps; field_energy and kinetic_energy (steps x nruns,
+ * may be NULL) get each run's 0.5*sum(E^2)*dV after the solve and 0.5*m*sum(v^2). */
+int pic_ens_run(pic_ens* ens, int steps, double* field_energy, double* kinetic_energy);
+int pic_ens_num_runs(pic_ens* ens, int* n);
+int pic_ens_info(pic_ens* ens, int run, pic_ens_run_info* info);
+int pic_ens_launch_count(pic_ens* ens, long long* n);
+int pic_ens_get_stream(pic_ens* ens, void** stream_out);
+/* Run `run`'s particles (positions in cell units, velocities; any pointer may be
+ * NULL) in their device order, and its rho and phi (N*N each). */
+int pic_ens_download_run(pic_ens* ens, int run, double* x, double* y, double* vx, double* vy, double* rho,
+                         double* phi);
+
 /* ---- 3x3 periodic convolution layers on the tensor cores (BF16, FP32 accumulate) ----
  *
  * No counterpart in the reference: the layers of the learned warm start for the

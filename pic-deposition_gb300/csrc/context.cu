@@ -322,7 +322,8 @@ int pic_gpu_create(const pic_domain* dom, size_t capacity, int device, pic_ctx**
         return fail(PIC_ERR_ARG, "pic_gpu_create: grid must be Nx,Ny >= 1 and Lx,Ly > 0");
     if ((size_t)dom->Nx * (size_t)dom->Ny > (size_t)1 << 30)
         return fail(PIC_ERR_ARG, "pic_gpu_create: more than 2^30 cells");
-    if (capacity > ((size_t)1 << 31) - 1) return fail(PIC_ERR_ARG, "pic_gpu_create: capacity above 2^31-1");
+    // particle indices are 32-bit on the device; int64 cell sums hold 2^39 particles of 2^24 units
+    if (capacity > ((size_t)1 << 32) - 4096) return fail(PIC_ERR_ARG, "pic_gpu_create: capacity above 2^32-4096");
     int ndev = 0;
     PIC_CUDA_TRY(cudaGetDeviceCount(&ndev));
     if (device < 0 || device >= ndev) return fail(PIC_ERR_ARG, "pic_gpu_create: no such device");

@@ -151,6 +151,94 @@ def nn_conv3x3(op: int, x: np.ndarray, weight=None, bias=None, aux=None, cin: in
     return out
 
 
+class EnsMember(C.Structure):
+    _fields_ = [("N", C.c_int), ("ppc", C.c_int), ("seed", C.c_uint)]
+
+
+class EnsConfig(C.Structure):
+    _fields_ = [("dt", C.c_double), ("amplitude", C.c_double), ("vth", C.c_double), ("sort_interval", C.c_int),
+                ("use_graph", C.c_int), ("seed", C.c_uint)]
+
+
+class EnsRunInfo(C.Structure):
+    _fields_ = [("N", C.c_int), ("ppc", C.c_int), ("particles", C.c_size_t), ("tile_w", C.c_int),
+                ("tile_h", C.c_int)]
+
+
+_SIGS += [
+    ("pic_ens_create", [C.POINTER(EnsMember), C.c_int, C.POINTER(EnsConfig), C.c_int, C.POINTER(_vp)]),
+    ("pic_ens_destroy", [_vp]),
+    ("pic_ens_run", [_vp, C.c_int, _vp, _vp]),
+    ("pic_ens_num_runs", [_vp, C.POINTER(C.c_int)]),
+    ("pic_ens_info", [_vp, C.c_int, C.POINTER(EnsRunInfo)]),
+    ("pic_ens_launch_count", [_vp, C.POINTER(C.c_longlong)]),
+    ("pic_ens_get_stream", [_vp, C.POINTER(_vp)]),
+    ("pic_ens_download_run", [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+]
+
+
+class Ensemble:
+    """A batch of independent Langmuir runs (pic_ens_*). `runs`: list of (N, ppc, seed).
+    Runs are reordered by grid size; info(r) gives run r's setup in that order."""
+
+    def __init__(self, runs, dt=0.1, amplitude=0.01, vth=0.05, sort_interval=20, use_graph=True, seed=1,
+                 device=0):
+        arr = (EnsMember * len(runs))(*[EnsMember(int(n), int(p), int(s)) for n, p, s in runs])
+        cfg = EnsConfig(float(dt), float(amplitude), float(vth), int(sort_interval), int(use_graph), int(seed))
+        h = _vp()
+        _check(lib().pic_ens_create(arr, len(runs), C.byref(cfg), int(device), C.byref(h)))
+        self.h = h
+        self.nruns = len(runs)
+
+    def close(self):
+        if self.h:
+            lib().pic_ens_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def run(self, steps):
+        fe = np.zeros((max(steps, 1), self.nruns))
+        ke = np.zeros((max(steps, 1), self.nruns))
+        _check(lib().pic_ens_run(self.h, int(steps), _ptr(fe), _ptr(ke)))
+        return fe[:steps], ke[:steps]
+
+    def info(self, r):
+        i = EnsRunInfo()
+        _check(lib().pic_ens_info(self.h, int(r), C.byref(i)))
+        return {"N": i.N, "ppc": i.ppc, "particles": i.particles, "tile": (i.tile_w, i.tile_h)}
+
+    def launch_count(self):
+        n = C.c_longlong()
+        _check(lib().pic_ens_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def stream(self):
+        s = _vp()
+        _check(lib().pic_ens_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def download_run(self, r):
+        inf = self.info(r)
+        n, g = inf["particles"], inf["N"] ** 2
+        out = {k: np.zeros(n) for k in ("x", "y", "vx", "vy")}
+        rho, phi = np.zeros(g), np.zeros(g)
+        _check(lib().pic_ens_download_run(self.h, int(r), _ptr(out["x"]), _ptr(out["y"]), _ptr(out["vx"]),
+                                          _ptr(out["vy"]), _ptr(rho), _ptr(phi)))
+        out["rho"], out["phi"] = rho, phi
+        return out
+
+
 class PinnedArray:
     """A page-locked host buffer (pic_gpu_host_alloc) viewed as a numpy array."""
 

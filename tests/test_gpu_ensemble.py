@@ -1,0 +1,82 @@
+"""The batched ensemble (pic_ens_*): each run equals the same run advanced alone
+through pic_gpu_run; the CUDA graph and the cell-sort interval change no bit;
+the runs oscillate at the plasma frequency."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RUNS = [(256, 4, 11), (128, 16, 12), (128, 4, 13), (256, 16, 14)]
+DT = 0.1
+
+
+def single_run(pg, st0, info, steps):
+    """The ensemble member's initial state advanced alone (scheme CIC, FFT, background 1)."""
+    N, ppc = info["N"], info["ppc"]
+    n = len(st0["x"])
+    q = np.full(n, -1.0 / ppc)
+    m = np.full(n, 1.0 / ppc)
+    with pg.Context(N, N, float(N), float(N), n) as c:
+        c.upload(st0["x"], st0["y"], q, st0["vx"], st0["vy"], m)
+        c.run(steps, scheme=1, dt=DT, background=1.0, sort_interval=0, use_graph=False, poisson=0)
+        p = c.download()
+        rho = c.rho()
+        phi, _, _ = c.fields()
+    return p, rho, phi
+
+
+@pytest.mark.parametrize("steps", [1, 6])
+def test_members_match_single_runs(pg, steps):
+    with pg.Ensemble(RUNS, dt=DT, sort_interval=0, use_graph=False) as e:
+        st0 = [e.download_run(r) for r in range(len(RUNS))]
+        infos = [e.info(r) for r in range(len(RUNS))]
+        e.run(steps)
+        after = [e.download_run(r) for r in range(len(RUNS))]
+    for r in range(len(RUNS)):
+        p, rho, phi = single_run(pg, st0[r], infos[r], steps)
+        a = after[r]
+        if steps == 1:
+            # first step: same positions (the first gather sees E = 0) and the same charge, bit for bit
+            assert np.array_equal(a["x"], p["x"]) and np.array_equal(a["y"], p["y"])
+            assert np.array_equal(a["rho"], rho.ravel())
+        else:
+            assert np.max(np.abs(a["x"] - p["x"])) < 1e-4 and np.max(np.abs(a["y"] - p["y"])) < 1e-4
+            assert np.max(np.abs(a["rho"] - rho.ravel())) <= 1e-3 * np.max(np.abs(rho))
+        assert np.allclose(a["phi"], phi.ravel(), rtol=1e-9, atol=1e-9 * np.max(np.abs(phi)))
+
+
+def test_graph_and_sort_interval_change_nothing(pg):
+    res = []
+    for sort_interval, graph in [(0, False), (3, True)]:
+        with pg.Ensemble(RUNS, dt=DT, sort_interval=sort_interval, use_graph=graph) as e:
+            fe, ke = e.run(9)
+            states = [e.download_run(r) for r in range(len(RUNS))]
+            tiles = [e.info(r)["tile"] for r in range(len(RUNS))]
+        res.append((fe, ke, states, tiles))
+    (fe0, ke0, s0, _), (fe1, ke1, s1, tiles) = res
+    assert np.array_equal(fe0, fe1)
+    for a, b in zip(s0, s1):
+        assert np.array_equal(a["rho"], b["rho"]) and np.array_equal(a["phi"], b["phi"])
+        ka = np.lexsort((a["vy"], a["vx"], a["y"], a["x"]))
+        kb = np.lexsort((b["vy"], b["vx"], b["y"], b["x"]))
+        for k in ("x", "y", "vx", "vy"):
+            assert np.array_equal(a[k][ka], b[k][kb])
+    assert np.allclose(ke0, ke1, rtol=1e-12)
+    assert all(w >= 1 and h >= 1 for w, h in tiles)
+
+
+def test_mode_growth_rate(pg):
+    """The reference's force sign (v += -(q/m) E dt with E = -grad phi and
+    -lap phi = rho, src/deposition/deposition.cpp:354-355, poisson_fft.cpp:45-94)
+    makes like charges attract, so a cold density perturbation grows as
+    cosh(omega_p t) instead of oscillating (the reference's own Langmuir
+    validation reports passed = false, src/pic/validation.cpp:245). With
+    omega_p = 1 the field energy grows like cosh^2(t): its mean log-slope over
+    t in [1.5, 4] is (ln cosh^2(4) - ln cosh^2(1.5)) / 2.5 = 1.96."""
+    steps = 41
+    with pg.Ensemble([(128, 16, 1), (128, 64, 2), (256, 16, 3)], dt=DT, amplitude=0.01, vth=0.01,
+                     sort_interval=20) as e:
+        fe, _ = e.run(steps)
+    for r in range(fe.shape[1]):
+        slope = (np.log(fe[39, r]) - np.log(fe[14, r])) / (25 * DT)
+        assert 1.7 < slope < 2.2, (r, slope)
