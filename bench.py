@@ -518,6 +518,49 @@ def run_ensemble(args):
     return out
 
 
+# tensor-core work of the warm-start network per 512x512 sample, as executed
+# (first layer 16 input channels, last layer 16 output channels, of which one is used)
+NN_LAYERS = [(16, 32), (32, 32), (32, 32), (32, 32), (32, 32), (32, 16)]
+
+
+def run_nn_profile(args):
+    """Throughput of the tcgen05 convolution kernels: forward, input gradient and
+    weight gradient of the warm-start network on a batch of 512x512 fields."""
+    import pic_gb300 as pg
+
+    B, N = args.nn_batch, GS_N
+    P = B * N * N
+    rng = np.random.default_rng(3)
+    inp = rng.normal(size=(B, N, N)).astype(np.float32)
+    tgt = rng.normal(size=(B, N, N)).astype(np.float32)
+    with pg.Context(N, N, float(N), float(N), 16) as c:
+        c.ws_init(seed=1)
+        for _ in range(3):
+            c.ws_loss_grad(inp, tgt)
+        c.profile(True)
+        reps = args.nn_reps
+        for _ in range(reps):
+            c.ws_loss_grad(inp, tgt)
+        prof = {k: c.profile_read(k) for k in ("conv_fwd", "conv_dgrad", "conv_wgrad")}
+        c.profile(False)
+    flops_fwd = sum(2.0 * P * 9 * ci * co for ci, co in NN_LAYERS)
+    flops_dgrad = sum(2.0 * P * 9 * ci * co for ci, co in NN_LAYERS[1:])
+    flops_wgrad = flops_fwd
+    peak = 1890.5
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        pass
+    out = {"workload": f"conv3x3_net_{N}x{N}_batch{B}", "batch": B, "peak_bf16_tflops": peak}
+    for k, fl in (("conv_fwd", flops_fwd), ("conv_dgrad", flops_dgrad), ("conv_wgrad", flops_wgrad)):
+        ms, n = prof[k]
+        t = ms / reps
+        out[k] = {"ms_per_pass": t, "launches_per_pass": n / reps, "tflops": fl / (t * 1e-3) / 1e12,
+                  "frac_of_bf16_peak": fl / (t * 1e-3) / 1e12 / peak}
+    return out
+
+
 def run_gs_study(args):
     """Time to a 1e-8 relative residual of red-black Gauss-Seidel from three
     starting guesses (previous phi; cubic extrapolation; extrapolation plus the
@@ -571,6 +614,9 @@ def main():
     ap.add_argument("--deposit-only", action="store_true", help="reduced run for profilers")
     ap.add_argument("--gs-only", action="store_true", help="only the Gauss-Seidel warm-start study")
     ap.add_argument("--no-gs", action="store_true", help="skip the Gauss-Seidel warm-start study")
+    ap.add_argument("--nn-only", action="store_true", help="only the convolution-kernel throughput")
+    ap.add_argument("--nn-batch", type=int, default=8)
+    ap.add_argument("--nn-reps", type=int, default=5)
     ap.add_argument("--ens-only", action="store_true", help="only the batched ensemble")
     ap.add_argument("--no-ens", action="store_true", help="skip the batched ensemble")
     ap.add_argument("--ens-runs", type=int, default=64)
@@ -592,6 +638,9 @@ def main():
     if args.ens_only:
         print(json.dumps(run_ensemble(args)), flush=True)
         return
+    if args.nn_only:
+        print(json.dumps(run_nn_profile(args)), flush=True)
+        return
     d = Dist()
     if args.deposit_only:
         run_deposit_only(args, d)
@@ -604,6 +653,7 @@ def main():
                 res["ensemble"] = run_ensemble(args)
             if not args.no_gs:
                 res["gs_warm_start"] = run_gs_study(args)
+                res["conv_kernels"] = run_nn_profile(args)
     finally:
         d.close()
     if res is not None:

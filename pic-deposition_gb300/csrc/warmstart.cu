@@ -235,8 +235,11 @@ int ws_forward(pic_ctx* c, int nb) {
     for (int l = 0; l < NL; ++l) {
         picnn::ConvLaunch a{s->act[l], s->img_f[l], s->params + s->off_b[l], nullptr,
                             l < NL - 1 ? (void*)s->act[l + 1] : (void*)s->out, nb, s->H, s->W, rows, s->err};
-        PIC_TRY(picnn::launch_conv(a, CIN[l], COUT[l], l < NL - 1 ? picnn::EPI_BIAS_RELU : picnn::EPI_BIAS_OUT,
-                                   c->stream));
+        prof_begin(c, "conv_fwd");
+        const int rc = picnn::launch_conv(a, CIN[l], COUT[l], l < NL - 1 ? picnn::EPI_BIAS_RELU : picnn::EPI_BIAS_OUT,
+                                          c->stream);
+        prof_end(c);
+        PIC_TRY(rc);
         c->launches++;
     }
     return PIC_OK;
@@ -254,14 +257,20 @@ int ws_backward(pic_ctx* c, int nb) {
     uint16_t* bufs[2] = {s->dza, s->dzb};
     for (int l = NL - 1; l >= 0; --l) {
         picnn::WgradLaunch w{s->act[l], g, s->partials, nb, s->H, s->W, upc, s->err};
-        PIC_TRY(picnn::launch_wgrad(w, CIN[l], COUT[l], grid, c->stream));
+        prof_begin(c, "conv_wgrad");
+        const int rw = picnn::launch_wgrad(w, CIN[l], COUT[l], grid, c->stream);
+        prof_end(c);
+        PIC_TRY(rw);
         PIC_TRY(picnn::reduce_wgrad(s->partials, grid, CIN[l], COUT[l], s->grad + s->off_w[l], s->grad + s->off_b[l],
                                     c->stream));
         c->launches += 2;
         if (l > 0) {
             uint16_t* next = bufs[l & 1];
             picnn::ConvLaunch a{g, s->img_b[l], nullptr, s->act[l], next, nb, s->H, s->W, rows, s->err};
-            PIC_TRY(picnn::launch_conv(a, COUT[l], CIN[l], picnn::EPI_MASK, c->stream));
+            prof_begin(c, "conv_dgrad");
+            const int rd = picnn::launch_conv(a, COUT[l], CIN[l], picnn::EPI_MASK, c->stream);
+            prof_end(c);
+            PIC_TRY(rd);
             c->launches++;
             g = next;
         }
