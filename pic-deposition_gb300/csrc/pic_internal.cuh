@@ -98,6 +98,8 @@ struct pic_ctx {
     double* red_out = nullptr;
     // red-black Gauss-Seidel
     double *rb_b = nullptr, *rb_partial = nullptr, *rb_scalars = nullptr;
+    double* rb_ps = nullptr;   // persistent solve: partial sums, barrier, results
+    int rbgs_persistent = 1;   // use the one-launch solve where it applies
     int last_rbgs_iters = 0;
     double last_rbgs_resid = 0.0, first_rbgs_resid = 0.0;
     // learned warm start (warmstart.cu)

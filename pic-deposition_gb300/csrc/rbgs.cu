@@ -17,6 +17,8 @@
 // Sums (mean, residual norms) use a fixed two-level tree, so results are
 // identical run to run. Odd Nx or Ny is rejected: the colouring would not be a
 // valid red-black split across the periodic seam.
+#include <cstring>
+
 #include "pic_internal.cuh"
 
 namespace picgb {
@@ -184,7 +186,229 @@ static int rb_finish(pic_ctx* c) {
     return efield_from_phi(c);
 }
 
-// Solves with the residual checked on the host every `check_every` sweeps.
+// ---- one cooperative launch per solve ---------------------------------------
+// Each CTA owns a tw x th tile of phi and keeps it, with a halo of PS_HALO
+// cells and the matching piece of b, in shared memory. Between two exchanges it
+// performs PS_HALO half-sweeps (two full red-black sweeps) on its extended
+// tile, the updated region shrinking by one cell per half-sweep, so the owned
+// cells end with exactly the values the one-launch-per-colour path computes
+// (same update, same operation order, same colour order). Then it writes its
+// owned cells back, waits at a grid-wide barrier and reloads its halo. The
+// residual is checked every check_every sweeps: per-CTA sums of r^2 and b^2,
+// a barrier, and every CTA adds the partials in index order and takes the
+// same decision. Barriers give up after about one second (PIC_ERR_TIMEOUT).
+constexpr int PS_THREADS = RB_THREADS;
+constexpr int PS_HALO = 4;
+constexpr int PS_MAX_BLOCKS = 4096;
+
+struct PsArgs {
+    RbArgs a;
+    int tw, th, tiles_x, ew, eh;
+    double tol;
+    int max_iters, check_every;
+    double* partial;  // [2 * blocks]
+    unsigned* bar;    // [0] arrivals, [1] generation
+    int* err;
+    double* out;      // [0] sweeps, [1] residual, [2] first residual
+};
+
+__device__ __forceinline__ uint64_t ps_time_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ bool ps_barrier(unsigned* bar, int* err) {
+    __syncthreads();
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned* vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const uint64_t t0 = ps_time_ns();
+            while (*vgen == gen)
+                if (ps_time_ns() - t0 > 1000000000ull) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+__device__ __forceinline__ int ps_wrap(int i, int n) {
+    const int r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+__global__ void __launch_bounds__(PS_THREADS) rbgs_persistent(PsArgs p) {
+    extern __shared__ double psm[];
+    const int E = p.ew * p.eh;
+    double* sphi = psm;
+    double* sb = psm + E;
+    __shared__ double tot[2];
+    const RbArgs& a = p.a;
+    const int tx = blockIdx.x % p.tiles_x, ty = blockIdx.x / p.tiles_x;
+    const int ox = tx * p.tw - PS_HALO, oy = ty * p.th - PS_HALO;
+    for (int i = threadIdx.x; i < E; i += PS_THREADS) {
+        const int ly = i / p.ew, lx = i - ly * p.ew;
+        const size_t g = (size_t)ps_wrap(oy + ly, a.Ny) * a.Nx + ps_wrap(ox + lx, a.Nx);
+        sb[i] = a.b[g];
+        sphi[i] = a.phi[g];
+    }
+    __syncthreads();
+    const int nown = p.tw * p.th;
+    double bb = 0.0;
+    for (int t = threadIdx.x; t < nown; t += PS_THREADS) {
+        const int i = (PS_HALO + t / p.tw) * p.ew + PS_HALO + t % p.tw;
+        bb = __dadd_rn(bb, __dmul_rn(sb[i], sb[i]));
+    }
+    bb = rb_block_sum(bb);
+    if (threadIdx.x == 0) p.partial[2 * blockIdx.x + 1] = bb;
+    int it = 0;
+    double res = 0.0, res0 = -1.0;
+    for (;;) {
+        if (it % p.check_every == 0 || it >= p.max_iters) {
+            double rr = 0.0;
+            for (int t = threadIdx.x; t < nown; t += PS_THREADS) {
+                const int i = (PS_HALO + t / p.tw) * p.ew + PS_HALO + t % p.tw;
+                const double we = __dadd_rn(sphi[i - 1], sphi[i + 1]);
+                const double sn = __dadd_rn(sphi[i - p.ew], sphi[i + p.ew]);
+                const double ap = __dsub_rn(__dsub_rn(__dmul_rn(a.denom, sphi[i]), __dmul_rn(we, a.ix2)),
+                                            __dmul_rn(sn, a.iy2));
+                const double r = __dsub_rn(sb[i], ap);
+                rr = __dadd_rn(rr, __dmul_rn(r, r));
+            }
+            rr = rb_block_sum(rr);
+            if (threadIdx.x == 0) p.partial[2 * blockIdx.x] = rr;
+            if (!ps_barrier(p.bar, p.err)) break;
+            if (threadIdx.x == 0) {
+                double s1 = 0.0, s2 = 0.0;
+                for (unsigned k = 0; k < gridDim.x; ++k) {
+                    s1 = __dadd_rn(s1, p.partial[2 * k]);
+                    s2 = __dadd_rn(s2, p.partial[2 * k + 1]);
+                }
+                tot[0] = s1;
+                tot[1] = s2;
+            }
+            __syncthreads();
+            res = tot[1] > 0.0 ? sqrt(tot[0] / tot[1]) : sqrt(tot[0]);
+            if (res0 < 0.0) res0 = res;
+            if (res <= p.tol || it >= p.max_iters) break;
+        }
+        for (int k = 0; k < PS_HALO; ++k) {
+            const int color = k & 1;
+            const int lo = k + 1;
+            const int rows = p.eh - 2 * lo, cols = p.ew - 2 * lo;
+            const int half = (cols + 1) >> 1;
+            for (int t = threadIdx.x; t < rows * half; t += PS_THREADS) {
+                const int r = t / half, m = t - r * half;
+                const int ly = lo + r;
+                const int lx = lo + (((ox + lo + oy + ly) & 1) ^ color) + 2 * m;
+                if (lx >= p.ew - lo) continue;
+                const int i = ly * p.ew + lx;
+                const double we = __dadd_rn(sphi[i - 1], sphi[i + 1]);
+                const double sn = __dadd_rn(sphi[i - p.ew], sphi[i + p.ew]);
+                sphi[i] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(we, a.ix2), __dmul_rn(sn, a.iy2)), sb[i]),
+                                    a.inv_denom);
+            }
+            __syncthreads();
+        }
+        it += PS_HALO / 2;
+        for (int t = threadIdx.x; t < nown; t += PS_THREADS) {
+            const int ly = PS_HALO + t / p.tw, lx = PS_HALO + t % p.tw;
+            a.phi[(size_t)(oy + ly) * a.Nx + (ox + lx)] = sphi[ly * p.ew + lx];
+        }
+        if (!ps_barrier(p.bar, p.err)) break;
+        for (int i = threadIdx.x; i < E; i += PS_THREADS) {
+            const int ly = i / p.ew, lx = i - ly * p.ew;
+            if (ly >= PS_HALO && ly < PS_HALO + p.th && lx >= PS_HALO && lx < PS_HALO + p.tw) continue;
+            sphi[i] = a.phi[(size_t)ps_wrap(oy + ly, a.Ny) * a.Nx + ps_wrap(ox + lx, a.Nx)];
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        p.out[0] = (double)it;
+        p.out[1] = res;
+        p.out[2] = res0;
+    }
+}
+
+static int largest_divisor_tile(int n, const int* cand, int ncand) {
+    for (int k = 0; k < ncand; ++k)
+        if (cand[k] <= n && n % cand[k] == 0) return cand[k];
+    return 0;
+}
+
+// Solves in one cooperative launch when the grid tiles evenly and every CTA can
+// be resident; returns PIC_ERR_UNSUPPORTED (nothing queued) otherwise.
+static int rbgs_solve_persistent(pic_ctx* c, const RbArgs& a, double tol, int max_iters, int check_every, int* it,
+                                 double* res) {
+    if ((check_every & 1) || (max_iters & 1)) return PIC_ERR_UNSUPPORTED;
+    static const int cw[] = {64, 32, 16, 8, 4, 2};
+    static const int ch[] = {32, 16, 8, 4, 2};
+    const int tw = largest_divisor_tile(c->Nx, cw, 6), th = largest_divisor_tile(c->Ny, ch, 5);
+    if (!tw || !th) return PIC_ERR_UNSUPPORTED;
+    const int tiles_x = c->Nx / tw, blocks = tiles_x * (c->Ny / th);
+    const int ew = tw + 2 * PS_HALO, eh = th + 2 * PS_HALO;
+    const size_t smem = (size_t)2 * ew * eh * sizeof(double);
+    if (blocks > PS_MAX_BLOCKS || smem > 200 * 1024) return PIC_ERR_UNSUPPORTED;
+    static size_t smem_set = 0;
+    if (smem > 48 * 1024 && smem > smem_set) {
+        if (cudaFuncSetAttribute(rbgs_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return PIC_ERR_UNSUPPORTED;
+        smem_set = smem;
+    }
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rbgs_persistent, PS_THREADS, smem);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (per_sm * sms < blocks) return PIC_ERR_UNSUPPORTED;
+    int rc = PIC_OK;
+    if (!c->rb_ps) c->rb_ps = (double*)dalloc((2 * PS_MAX_BLOCKS + 8) * sizeof(double), &rc);
+    if (rc) return rc;
+    double* out = c->rb_ps + 2 * PS_MAX_BLOCKS;
+    unsigned* bar = reinterpret_cast<unsigned*>(out + 4);
+    int* err = reinterpret_cast<int*>(out + 5);
+    PIC_CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), c->stream));
+    PIC_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+    PsArgs p{a, tw, th, tiles_x, ew, eh, tol, max_iters, check_every, c->rb_ps, bar, err, out};
+    cudaLaunchConfig_t lc{};
+    lc.gridDim = dim3(blocks);
+    lc.blockDim = dim3(PS_THREADS);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = c->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    PIC_CUDA_TRY(cudaLaunchKernelEx(&lc, rbgs_persistent, p));
+    c->launches++;
+    double h[6];
+    PIC_CUDA_TRY(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    PIC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    int herr = 0;
+    std::memcpy(&herr, &h[5], sizeof(int));
+    if (herr) return fail(PIC_ERR_TIMEOUT, "red-black Gauss-Seidel: a grid-wide barrier timed out");
+    *it = (int)h[0];
+    *res = h[1];
+    c->first_rbgs_resid = h[2];
+    return PIC_OK;
+}
+
+// Solves with the residual checked every `check_every` sweeps: in one
+// cooperative launch where possible, else one launch per colour with the
+// residual read on the host.
 int rbgs_solve(pic_ctx* c, double tol, int max_iters, int check_every, int* iters_out, double* resid_out) {
     if ((c->Nx & 1) || (c->Ny & 1)) return fail(PIC_ERR_UNSUPPORTED, "red-black Gauss-Seidel needs even Nx and Ny");
     if (max_iters < 0) return fail(PIC_ERR_ARG, "max_iters < 0");
@@ -195,7 +419,10 @@ int rbgs_solve(pic_ctx* c, double tol, int max_iters, int check_every, int* iter
     int it = 0;
     double res = 0.0;
     prof_begin(c, "rbgs");
-    for (;;) {
+    const int prc = c->rbgs_persistent ? rbgs_solve_persistent(c, a, tol, max_iters, check_every, &it, &res)
+                                       : PIC_ERR_UNSUPPORTED;
+    if (prc != PIC_OK && prc != PIC_ERR_UNSUPPORTED) return prc;
+    for (; prc == PIC_ERR_UNSUPPORTED;) {
         PIC_TRY(rb_residual_async(c, a));
         double s[3];
         PIC_CUDA_TRY(cudaMemcpyAsync(s, c->rb_scalars, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
@@ -253,6 +480,7 @@ int rbgs_solve_async(pic_ctx* c, double tol, int max_iters, int check_every) {
 }
 
 void release_rbgs(pic_ctx* c) {
+    dfree(c->rb_ps);
     dfree(c->rb_b);
     dfree(c->rb_partial);
     dfree(c->rb_scalars);

@@ -119,6 +119,22 @@ def test_rbgs_fixed_sweeps_close_to_oracle(pg, port):
     assert np.max(np.abs(phi - want)) <= 1e-12 * np.max(np.abs(want))
 
 
+@pytest.mark.parametrize("nx,ny", [(64, 48), (512, 512), (16, 8)])
+def test_rbgs_one_launch_equals_per_colour_launches(pg, nx, ny):
+    """The one-launch solve (even check_every and max_iters) and the per-colour
+    launches (odd check_every) give the same phi bit for bit after the same sweeps."""
+    rng = np.random.default_rng(2)
+    rho = rng.normal(size=nx * ny)
+    out = []
+    for check_every in (40, 5):
+        with pg.Context(nx, ny, 1.0, 1.0, 1) as c:
+            c.set_rho(rho)
+            it, _ = c.poisson_rbgs(tol=0.0, max_iters=40, warm_start=False, check_every=check_every)
+            out.append((it, c.fields()[0]))
+    assert out[0][0] == out[1][0] == 40
+    assert np.array_equal(out[0][1], out[1][1])
+
+
 def test_rbgs_odd_grid_rejected(pg):
     with pg.Context(33, 32, 1.0, 1.0, 1) as c:
         c.set_rho(np.zeros(33 * 32))
