@@ -561,6 +561,39 @@ def run_nn_profile(args):
     return out
 
 
+def run_config3(args):
+    """Full electrostatic time step at 2048x2048 with 100 particles per cell
+    (419,430,400 particles): two equal beams vx = +-0.2, vth = 0.01, uniform
+    positions (the reference's two-stream conventions: charge -1/N, m = 1,
+    background 1/V), TSC, cell sort every 10 steps, FFT Poisson, fused graph steps."""
+    import pic_gb300 as pg
+
+    N, ppc = 2048, 100
+    n = N * N * ppc
+    steps, dt = args.c3_steps, 0.1
+    out = {"workload": f"timestep_twostream_tsc_{N}x{N}_{ppc}ppc", "particles": n, "steps": steps, "dt": dt,
+           "scheme": "TSC", "sort_interval": 10, "poisson": "FFT"}
+    with pg.Context(N, N, float(N), float(N), n) as c:
+        c.generate(n, vth=0.01, v0=0.2, charge=-1.0 / n, mass=1.0, seed=2024)
+        bg = 1.0 / (N * N)
+        c.run(10, scheme=2, dt=dt, background=bg, sort_interval=10, use_graph=True)  # warm-up, graph capture
+        c.generate(n, vth=0.01, v0=0.2, charge=-1.0 / n, mass=1.0, seed=2024)
+        ev = CudaEvents()
+        e0, e1 = ev.event(), ev.event()
+        ev.record(e0, c.stream())
+        h = c.run(steps, scheme=2, dt=dt, background=bg, sort_interval=10, use_graph=True)
+        ev.record(e1, c.stream())
+        ms = ev.elapsed_ms(e0, e1)
+    e = h[:, 5]
+    drift = (e - e[0]) / abs(e[0])
+    marks = sorted({0, steps // 4, steps // 2, 3 * steps // 4, steps - 1})
+    out.update({"ms_per_step": ms / steps, "particle_steps_per_s": n * steps / (ms * 1e-3),
+                "energy_drift_at_steps": {str(k): float(drift[k]) for k in marks},
+                "max_abs_energy_drift": float(np.max(np.abs(drift))),
+                "max_charge_error": float(np.max(h[:, 0]))})
+    return out
+
+
 def run_gs_study(args):
     """Time to a 1e-8 relative residual of red-black Gauss-Seidel from three
     starting guesses (previous phi; cubic extrapolation; extrapolation plus the
@@ -614,6 +647,9 @@ def main():
     ap.add_argument("--deposit-only", action="store_true", help="reduced run for profilers")
     ap.add_argument("--gs-only", action="store_true", help="only the Gauss-Seidel warm-start study")
     ap.add_argument("--no-gs", action="store_true", help="skip the Gauss-Seidel warm-start study")
+    ap.add_argument("--c3-only", action="store_true", help="only the 2048^2 two-stream time step")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 2048^2 two-stream time step")
+    ap.add_argument("--c3-steps", type=int, default=200)
     ap.add_argument("--nn-only", action="store_true", help="only the convolution-kernel throughput")
     ap.add_argument("--nn-batch", type=int, default=8)
     ap.add_argument("--nn-reps", type=int, default=5)
@@ -641,6 +677,9 @@ def main():
     if args.nn_only:
         print(json.dumps(run_nn_profile(args)), flush=True)
         return
+    if args.c3_only:
+        print(json.dumps(run_config3(args)), flush=True)
+        return
     d = Dist()
     if args.deposit_only:
         run_deposit_only(args, d)
@@ -651,6 +690,8 @@ def main():
         if res is not None and args.impl != "reference" and d.ws == 1:
             if not args.no_ens:
                 res["ensemble"] = run_ensemble(args)
+            if not args.no_c3:
+                res["timestep_2048"] = run_config3(args)
             if not args.no_gs:
                 res["gs_warm_start"] = run_gs_study(args)
                 res["conv_kernels"] = run_nn_profile(args)

@@ -118,6 +118,25 @@ int pic_gpu_host_free(void* p);
  * particles unsorted. */
 int pic_gpu_upload_particles(pic_ctx* ctx, const double* x, const double* y, const double* vx, const double* vy,
                              const double* q, const double* m, size_t n);
+/* Generates particles on the device (no counterpart in the reference; for synthetic
+ * workloads too large to build on the host): x from the density
+ * 1 + amplitude*cos(2*pi*mode*x/Lx) (mode 0: uniform), y uniform, Maxwellian
+ * velocities of thermal speed vth per component, plus +v0 in x for the first
+ * half and -v0 for the second (two beams, as ParticlesSoA::initializeTwoStream,
+ * src/pic/particles_aos.cpp:142-160, when v0 != 0); every particle has the given
+ * charge and mass. Philox4x32-10 random numbers, so the set depends only on seed
+ * and n. Replaces the resident particles (n <= capacity); marks them unsorted. */
+typedef struct pic_gen_config {
+    size_t n;
+    double amplitude;
+    int mode;
+    double vth;
+    double v0;
+    double charge;
+    double mass;
+    unsigned seed;
+} pic_gen_config;
+int pic_gpu_generate(pic_ctx* ctx, const pic_gen_config* cfg);
 /* Downloads particles back to FP64 SoA (positions rebuilt as (ix+xr)*dx). Any pointer may be NULL. */
 int pic_gpu_download_particles(pic_ctx* ctx, double* x, double* y, double* vx, double* vy, double* q, double* m);
 /* Raw device layout, for bit-exact parity checks: any pointer may be NULL. */

@@ -217,24 +217,6 @@ struct ConvertArgs {
     DevStats* st;
 };
 
-// Domain::cellCoords (src/pic/domain.hpp:34-43) in FP64: w = x/dx, i = floor(w),
-// frac = w - i, i wrapped. When dx is a power of two, x * (1/dx) equals the
-// correctly rounded x/dx exactly and replaces the (slow) FP64 division. The
-// FP32 offset keeps the NGP choice frac >= 0.5 (ngp.cpp:116-117) exact: a frac
-// below 0.5 that rounds up to 0.5f is stored as the float just below 0.5.
-__device__ __forceinline__ bool cell_coord(double x, double d, double inv_d, int n, int* idx, float* off) {
-    const double w = inv_d != 0.0 ? __dmul_rn(x, inv_d) : __ddiv_rn(x, d);
-    if (!(fabs(w) < 1073741824.0)) return false;  // also rejects NaN/inf
-    const double f = floor(w);
-    int i = (int)f;
-    const double frac = __dsub_rn(w, (double)i);
-    float r = __double2float_rn(frac);
-    if (frac < 0.5 && r >= 0.5f) r = 0.49999997f;
-    *idx = wrap_i(i, n);
-    *off = r;
-    return true;
-}
-
 __global__ void convert_particles(ConvertArgs a) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     float aq = 0.0f, avx = 0.0f, avy = 0.0f;
@@ -273,7 +255,7 @@ __global__ void convert_particles(ConvertArgs a) {
 }
 
 // 1/d when d is a power of two (then x * (1/d) == x / d exactly), else 0.
-static double exact_reciprocal(double d) {
+double exact_reciprocal(double d) {
     int e = 0;
     const double mant = std::frexp(d, &e);
     return mant == 0.5 ? std::ldexp(1.0, 1 - e) : 0.0;

@@ -175,6 +175,8 @@ int solve_discrete_fft(pic_ctx* ctx, const double* b, double* phi);
 // Particle motion (push.cu).
 int move(pic_ctx* ctx, double dt, bool gather, bool push);
 void release_ws(pic_ctx* ctx);
+// 1/d when d is a power of two (then x * (1/d) == x / d exactly), else 0.
+double exact_reciprocal(double d);
 
 // Brackets a kernel launch with profiling events when enabled.
 void prof_begin(pic_ctx* ctx, const char* name);
@@ -209,6 +211,25 @@ __device__ __forceinline__ void set_dev_error(DevStats* st, int code, unsigned i
 }
 
 __device__ __forceinline__ float load_maxq(const DevStats* st) { return __uint_as_float(st->maxq_bits); }
+
+// Domain::cellCoords (src/pic/domain.hpp:34-43) in FP64: w = x/dx, i = floor(w),
+// frac = w - i, i wrapped. When dx is a power of two, x * (1/dx) equals the
+// correctly rounded x/dx exactly and replaces the (slow) FP64 division. The
+// FP32 offset keeps the NGP choice frac >= 0.5 (ngp.cpp:116-117) exact: a frac
+// below 0.5 that rounds up to 0.5f is stored as the float just below 0.5.
+__device__ __forceinline__ bool cell_coord(double x, double d, double inv_d, int n, int* idx, float* off) {
+    const double w = inv_d != 0.0 ? __dmul_rn(x, inv_d) : __ddiv_rn(x, d);
+    if (!(fabs(w) < 1073741824.0)) return false;  // also rejects NaN/inf
+    const double f = floor(w);
+    int i = (int)f;
+    const double frac = __dsub_rn(w, (double)i);
+    float r = __double2float_rn(frac);
+    if (frac < 0.5 && r >= 0.5f) r = 0.49999997f;
+    *idx = wrap_i(i, n);
+    *off = r;
+    return true;
+}
+
 
 // One unit of the int64 charge grid: max|q| * inv_vol * 2^-24 (FP64). The
 // resident charge is stored normalised, qn = q / max|q|, and a particle carries

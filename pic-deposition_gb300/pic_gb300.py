@@ -151,6 +151,15 @@ def nn_conv3x3(op: int, x: np.ndarray, weight=None, bias=None, aux=None, cin: in
     return out
 
 
+class GenConfig(C.Structure):
+    """pic_gen_config (include/pic_gb300.h)."""
+    _fields_ = [("n", C.c_size_t), ("amplitude", C.c_double), ("mode", C.c_int), ("vth", C.c_double),
+                ("v0", C.c_double), ("charge", C.c_double), ("mass", C.c_double), ("seed", C.c_uint)]
+
+
+_SIGS.append(("pic_gpu_generate", [_vp, C.POINTER(GenConfig)]))
+
+
 class EnsMember(C.Structure):
     _fields_ = [("N", C.c_int), ("ppc", C.c_int), ("seed", C.c_uint)]
 
@@ -441,6 +450,12 @@ class Context:
         _check(lib().pic_gpu_poisson_rbgs(self.h, float(tol), int(max_iters), int(warm_start), int(check_every),
                                           C.byref(it), C.byref(res)))
         return it.value, res.value
+
+    def generate(self, n, amplitude=0.0, mode=1, vth=0.0, v0=0.0, charge=-1.0, mass=1.0, seed=1):
+        """Device-side particles (pic_gpu_generate)."""
+        cfg = GenConfig(int(n), float(amplitude), int(mode), float(vth), float(v0), float(charge), float(mass),
+                        int(seed))
+        _check(lib().pic_gpu_generate(self.h, C.byref(cfg)))
 
     # ---- learned warm start (pic_gpu_ws_*) ----
     def ws_init(self, seed: int = 1, dataset_capacity: int = 0):
