@@ -577,6 +577,238 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_atomic(DepArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// TSC fast paths. Same values as stencil_values<TSC> bit for bit, fewer
+// instructions:
+//  * the weights are computed without branching on r < 0.5: with t = r (r < 0.5)
+//    or t = r - 1 (r >= 0.5), the three non-zero weights are 0.5*(0.5-t)^2,
+//    0.75-t^2, 0.5*(0.5+t)^2 at frame columns 0..2 or 1..3 (each operation gives
+//    the bits the branchy form gives: r - 1, 0.5 - t and 0.5 + t are exact there);
+//  * the node of largest weight is always in rows and columns 1..2 of the frame,
+//    so the remainder goes to one of 4 entries;
+//  * the 12 entries outside rows and columns 1..2 involve an outer weight <= 1/8,
+//    so |value| < 2^22 and rint is one FP32 add of 1.5*2^23 (round to nearest
+//    even on the integer grid): the accumulators keep those entries with the
+//    constant's bits added once per particle, and the per-run particle count
+//    removes them when a total is written out. The 4 central entries use F2I.
+// ---------------------------------------------------------------------------
+constexpr float TSC_MAGIC = 12582912.0f;     // 1.5 * 2^23
+constexpr uint32_t TSC_MAGIC_BITS = 0x4B400000u;
+
+__host__ __device__ constexpr bool tsc_central(int k) { return ((k >> 2) == 1 || (k >> 2) == 2) && ((k & 3) == 1 || (k & 3) == 2); }
+
+__device__ __forceinline__ void tsc_axis(float r, float (&X)[4], int& kmax) {
+    const bool s = r >= 0.5f;
+    const float t = s ? r - 1.0f : r;
+    const float dl = 0.5f - t, dr = 0.5f + t;
+    const float L = 0.5f * (dl * dl), Cw = 0.75f - t * t, R = 0.5f * (dr * dr);
+    X[0] = s ? 0.0f : L;
+    X[1] = s ? L : Cw;
+    X[2] = s ? Cw : R;
+    X[3] = s ? R : 0.0f;
+    kmax = X[2] > X[1] ? 2 : 1;
+}
+
+// Frame values: central entries exact, the others biased by TSC_MAGIC_BITS.
+__device__ __forceinline__ void tsc_values(float rx, float ry, float qn, uint32_t (&val)[16]) {
+    const float aq = qn * 16777216.0f;
+    const int A = __float2int_rn(aq);
+    float X[4], Y[4];
+    int kx, ky;
+    tsc_axis(rx, X, kx);
+    tsc_axis(ry, Y, ky);
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float ay = aq * Y[j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float p = ay * X[i];
+            const uint32_t v = tsc_central(j * 4 + i) ? (uint32_t)__float2int_rn(p) : __float_as_uint(p + TSC_MAGIC);
+            val[j * 4 + i] = v;
+            sum += v;
+        }
+    }
+    const uint32_t rem = (uint32_t)A - (sum - 12u * TSC_MAGIC_BITS);
+    val[5] += (ky == 1 && kx == 1) ? rem : 0u;
+    val[6] += (ky == 1 && kx == 2) ? rem : 0u;
+    val[9] += (ky == 2 && kx == 1) ? rem : 0u;
+    val[10] += (ky == 2 && kx == 2) ? rem : 0u;
+}
+
+// True total of entry q of a run of `cnt` particles.
+__device__ __forceinline__ int tsc_true(int q, uint32_t acc, uint32_t cnt) {
+    return tsc_central(q) ? (int)acc : (int)(acc - cnt * TSC_MAGIC_BITS);
+}
+
+// Sorted path for TSC (deposit_tiled with the values above).
+__global__ void __launch_bounds__(DEP_THREADS) deposit_tiled_tsc(DepArgs a) {
+    extern __shared__ long long sacc[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int SW = a.tile_w + 3;
+    const int tx = blockIdx.x % a.tiles_x, ty = blockIdx.x / a.tiles_x;
+    const int x0 = tx * a.tile_w, y0 = ty * a.tile_h;
+    const int tw = min(a.tile_w, a.Nx - x0), th = min(a.tile_h, a.Ny - y0);
+    const int nloc = (th + 3) * SW;
+    for (int i = threadIdx.x; i < nloc; i += DEP_THREADS) sacc[i] = 0;
+    __syncthreads();
+    const unsigned upto = (lane == 31) ? FULL : ((2u << lane) - 1u);
+    for (int r = warp; r < th; r += DEP_WARPS) {
+        const int iy = y0 + r;
+        const uint32_t rowbase = (uint32_t)iy * (uint32_t)a.Nx;
+        const uint32_t c0 = rowbase + (uint32_t)x0;
+        const uint32_t pbeg = a.offsets[c0], pend = a.offsets[c0 + tw];
+        const int lcol = -x0;  // local column of frame column 0 is ix + lcol (frame starts at ix - 1, halo 1)
+        uint32_t base = pbeg & ~3u;
+        Quad<S_TSC> cur, nxt;
+        load_quad<S_TSC>(a, base + 4u * lane, base + 4u * lane < pend, cur);
+        while (base < pend) {
+            const uint32_t nbase = base + 128u;
+            if (nbase < pend) load_quad<S_TSC>(a, nbase + 4u * lane, nbase + 4u * lane < pend, nxt);
+            uint32_t ckey = NO_CELL, cnt = 0;
+            uint32_t acc[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) acc[k] = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t p = base + 4u * lane + (uint32_t)k;
+                if (p >= pbeg && p < pend) {
+                    const uint32_t key = u4(cur.cell, k);
+                    if (key - c0 >= (uint32_t)tw) {
+                        set_dev_error(a.st, DEV_UNSORTED, p);
+                        continue;
+                    }
+                    uint32_t val[16];
+                    tsc_values(f4(cur.xr, k), f4(cur.yr, k), f4(cur.q, k), val);
+                    if (key != ckey) {
+                        if (ckey != NO_CELL) {
+                            const int lx = (int)(ckey - rowbase) + lcol;
+#pragma unroll
+                            for (int q = 0; q < 16; ++q) {
+                                const int v = tsc_true(q, acc[q], cnt);
+                                if (v != 0) sadd(sacc, (r + q / 4) * SW + lx + (q % 4), v);
+                            }
+                        }
+                        ckey = key;
+                        cnt = 1;
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) acc[q] = val[q];
+                    } else {
+                        ++cnt;
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) acc[q] += val[q];
+                    }
+                }
+            }
+            const uint32_t kprev = __shfl_up_sync(FULL, ckey, 1);
+            const unsigned H = __ballot_sync(FULL, lane == 0 || ckey != kprev);
+            const int segstart = 31 - __clz(H & upto);
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const bool take = lane - d >= segstart;
+                const uint32_t oc = __shfl_up_sync(FULL, cnt, d);
+                if (take) cnt += oc;
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const uint32_t o = __shfl_up_sync(FULL, acc[q], d);
+                    if (take) acc[q] += o;
+                }
+            }
+            const bool tail = (lane == 31) || ((H >> (lane + 1)) & 1u);
+            if (tail && ckey != NO_CELL) {
+                const int lx = (int)(ckey - rowbase) + lcol;
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int v = tsc_true(q, acc[q], cnt);
+                    if (v != 0) sadd(sacc, (r + q / 4) * SW + lx + (q % 4), v);
+                }
+            }
+            cur = nxt;
+            base = nbase;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nloc; i += DEP_THREADS) {
+        const long long v = sacc[i];
+        if (v != 0) {
+            const int ly = i / SW, lx = i % SW;
+            const int gx = wrap_i(x0 - 1 + lx, a.Nx), gy = wrap_i(y0 - 1 + ly, a.Ny);
+            atomicAdd(a.acc + (size_t)gy * a.Nx + gx, (unsigned long long)v);
+        }
+    }
+}
+
+// Any-order path for TSC (deposit_runs with the values above).
+__global__ void __launch_bounds__(DEP_THREADS) deposit_runs_tsc(DepArgs a) {
+    const int lane = threadIdx.x & 31;
+    const size_t gw = (size_t)blockIdx.x * DEP_WARPS + (threadIdx.x >> 5);
+    const size_t stride = (size_t)gridDim.x * DEP_WARPS * 128;
+    const uint32_t G = (uint32_t)a.Nx * (uint32_t)a.Ny;
+    const unsigned upto = (lane == 31) ? FULL : ((2u << lane) - 1u);
+    size_t base = gw * 128;
+    Quad<S_TSC> cur, nxt;
+    load_quad<S_TSC>(a, (uint32_t)(base + 4u * lane), base + 4u * lane < a.n, cur);
+    for (; base < a.n; base += stride) {
+        const size_t nbase = base + stride;
+        if (nbase < a.n) load_quad<S_TSC>(a, (uint32_t)(nbase + 4u * lane), nbase + 4u * lane < a.n, nxt);
+        uint32_t ckey = NO_CELL, cnt = 0;
+        uint32_t acc[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc[q] = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const size_t p = base + 4u * lane + (size_t)k;
+            if (p < a.n) {
+                const uint32_t key = u4(cur.cell, k);
+                if (key >= G) {
+                    set_dev_error(a.st, DEV_BAD_CELL, (unsigned)p);
+                    continue;
+                }
+                uint32_t val[16];
+                tsc_values(f4(cur.xr, k), f4(cur.yr, k), f4(cur.q, k), val);
+                if (key != ckey) {
+                    if (ckey != NO_CELL) {
+                        int t[16];
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) t[q] = tsc_true(q, acc[q], cnt);
+                        flush_global<S_TSC>(a, ckey, t);
+                    }
+                    ckey = key;
+                    cnt = 1;
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) acc[q] = val[q];
+                } else {
+                    ++cnt;
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) acc[q] += val[q];
+                }
+            }
+        }
+        const uint32_t kprev = __shfl_up_sync(FULL, ckey, 1);
+        const unsigned H = __ballot_sync(FULL, lane == 0 || ckey != kprev);
+        const int segstart = 31 - __clz(H & upto);
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const bool take = lane - d >= segstart;
+            const uint32_t oc = __shfl_up_sync(FULL, cnt, d);
+            if (take) cnt += oc;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const uint32_t o = __shfl_up_sync(FULL, acc[q], d);
+                if (take) acc[q] += o;
+            }
+        }
+        const bool tail = (lane == 31) || ((H >> (lane + 1)) & 1u);
+        if (tail && ckey != NO_CELL) {
+            int t[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) t[q] = tsc_true(q, acc[q], cnt);
+            flush_global<S_TSC>(a, ckey, t);
+        }
+        cur = nxt;
+    }
+}
+
 // One unit of the int64 grid (FP64).
 __global__ void fixed_unit(double inv_vol, const DevStats* st, double* unit_out) {
     *unit_out = charge_unit(st, inv_vol);
@@ -596,7 +828,10 @@ static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
         const size_t smem = (size_t)(a.tile_h + 3) * (a.tile_w + 3) * sizeof(long long);
         const unsigned tiles = (unsigned)(a.tiles_x * ((c->Ny + a.tile_h - 1) / a.tile_h));
         prof_begin(c, "deposit");
-        deposit_tiled<S><<<tiles, DEP_THREADS, smem, c->stream>>>(a);
+        if constexpr (S == S_TSC)
+            deposit_tiled_tsc<<<tiles, DEP_THREADS, smem, c->stream>>>(a);
+        else
+            deposit_tiled<S><<<tiles, DEP_THREADS, smem, c->stream>>>(a);
         prof_end(c);
         return check_launch(c, "deposit_tiled");
     }
@@ -608,7 +843,10 @@ static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
         if (blocks > cap) blocks = cap;
         if (blocks == 0) blocks = 1;
         prof_begin(c, "deposit");
-        deposit_runs<S><<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
+        if constexpr (S == S_TSC)
+            deposit_runs_tsc<<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
+        else
+            deposit_runs<S><<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
         prof_end(c);
         return check_launch(c, "deposit_runs");
     }
