@@ -56,6 +56,8 @@ struct RunDesc {
     uint32_t pbase;      // first particle
     uint32_t np;         // particles
     uint32_t tile_base;  // first CTA of the run in the tiled deposit
+    uint32_t en_base;    // first block of the run in the energy sums
+    uint32_t en_blocks;  // blocks of the run in the energy sums
     int N;
     int tile_w, tile_h, tiles_x;
     float maxq;          // |q| of the run's particles
@@ -208,30 +210,50 @@ __global__ void __launch_bounds__(ENS_THREADS) ens_step_kernel(StepArgs a) {
     const size_t nthreads = (size_t)gridDim.x * ENS_THREADS;
     const size_t tid = (size_t)blockIdx.x * ENS_THREADS + threadIdx.x;
 
-    if (a.do_move) {  // gather + push (push.cu move_particles<true, true>)
-        for (size_t p = tid; p < a.n; p += nthreads) {
-            const RunDesc& r = a.runs[find_run(pbase, a.nruns, (uint32_t)p)];
+    if (a.do_move) {  // gather + push (push.cu move_particles<true, true>), 4 particles per thread
+        for (int ri = 0; ri < a.nruns; ++ri) {
+            const RunDesc& r = a.runs[ri];
             const int N = r.N;
-            const uint32_t local = a.cell[p] - r.cell_base;
-            int iy = (int)(local / (uint32_t)N);
-            int ix = (int)(local - (uint32_t)iy * (uint32_t)N);
-            float rx = a.xr[p], ry = a.yr[p];
-            float vxx = a.vx[p], vyy = a.vy[p];
-            const int ixp = (ix + 1) % N, iyp = (iy + 1) % N;
             const size_t b0 = r.cell_base;
-            const size_t i00 = b0 + (size_t)iy * N + ix, i10 = b0 + (size_t)iy * N + ixp;
-            const size_t i01 = b0 + (size_t)iyp * N + ix, i11 = b0 + (size_t)iyp * N + ixp;
-            const float ex = interp_f(a.Exf, i00, i10, i01, i11, rx, ry);
-            const float ey = interp_f(a.Eyf, i00, i10, i01, i11, rx, ry);
-            vxx = vxx + (r.coef * ex) * a.dtf;
-            vyy = vyy + (r.coef * ey) * a.dtf;
-            a.vx[p] = vxx;
-            a.vy[p] = vyy;
-            drift_f(rx, ix, vxx, a.dtd, N);
-            drift_f(ry, iy, vyy, a.dtd, N);
-            a.xr[p] = rx;
-            a.yr[p] = ry;
-            a.cell[p] = r.cell_base + (uint32_t)iy * (uint32_t)N + (uint32_t)ix;
+            const size_t nq = r.np / 4, q0 = r.pbase / 4;  // particle counts and bases are multiples of 4
+            for (size_t qi = tid; qi < nq; qi += nthreads) {
+                const size_t p0 = (q0 + qi) * 4;
+                uint4 cl = *reinterpret_cast<const uint4*>(a.cell + p0);
+                float4 fx = *reinterpret_cast<const float4*>(a.xr + p0);
+                float4 fy = *reinterpret_cast<const float4*>(a.yr + p0);
+                float4 gx = *reinterpret_cast<const float4*>(a.vx + p0);
+                float4 gy = *reinterpret_cast<const float4*>(a.vy + p0);
+                uint32_t* pc = reinterpret_cast<uint32_t*>(&cl);
+                float *px = reinterpret_cast<float*>(&fx), *py = reinterpret_cast<float*>(&fy);
+                float *pvx = reinterpret_cast<float*>(&gx), *pvy = reinterpret_cast<float*>(&gy);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t local = pc[k] - r.cell_base;
+                    int iy = (int)(local / (uint32_t)N);
+                    int ix = (int)(local - (uint32_t)iy * (uint32_t)N);
+                    float rx = px[k], ry = py[k];
+                    float vxx = pvx[k], vyy = pvy[k];
+                    const int ixp = (ix + 1) % N, iyp = (iy + 1) % N;
+                    const size_t i00 = b0 + (size_t)iy * N + ix, i10 = b0 + (size_t)iy * N + ixp;
+                    const size_t i01 = b0 + (size_t)iyp * N + ix, i11 = b0 + (size_t)iyp * N + ixp;
+                    const float ex = interp_f(a.Exf, i00, i10, i01, i11, rx, ry);
+                    const float ey = interp_f(a.Eyf, i00, i10, i01, i11, rx, ry);
+                    vxx = vxx + (r.coef * ex) * a.dtf;
+                    vyy = vyy + (r.coef * ey) * a.dtf;
+                    drift_f(rx, ix, vxx, a.dtd, N);
+                    drift_f(ry, iy, vyy, a.dtd, N);
+                    pvx[k] = vxx;
+                    pvy[k] = vyy;
+                    px[k] = rx;
+                    py[k] = ry;
+                    pc[k] = r.cell_base + (uint32_t)iy * (uint32_t)N + (uint32_t)ix;
+                }
+                *reinterpret_cast<uint4*>(a.cell + p0) = cl;
+                *reinterpret_cast<float4*>(a.xr + p0) = fx;
+                *reinterpret_cast<float4*>(a.yr + p0) = fy;
+                *reinterpret_cast<float4*>(a.vx + p0) = gx;
+                *reinterpret_cast<float4*>(a.vy + p0) = gy;
+            }
         }
         if (a.do_deposit || a.do_convert)
             if (!grid_barrier(a.bar, a.err)) return;
@@ -288,11 +310,14 @@ __global__ void __launch_bounds__(ENS_THREADS) ens_step_kernel(StepArgs a) {
             if (!grid_barrier(a.bar, a.err)) return;
     }
     if (a.do_convert) {  // deposit.cu fixed_to_rho per run; clears the int64 grid
-        for (size_t g = tid; g < a.G; g += nthreads) {
-            const RunDesc& r = a.runs[find_run(cbase, a.nruns, (uint32_t)g)];
-            const long long v = (long long)a.acc[g];
-            a.rho[g] = __dadd_rn(__dmul_rn((double)v, r.unit), r.background);
-            a.acc[g] = 0ull;
+        for (int ri = 0; ri < a.nruns; ++ri) {
+            const RunDesc& r = a.runs[ri];
+            for (size_t i = tid; i < r.cells; i += nthreads) {
+                const size_t g = r.cell_base + i;
+                const long long v = (long long)a.acc[g];
+                a.rho[g] = __dadd_rn(__dmul_rn((double)v, r.unit), r.background);
+                a.acc[g] = 0ull;
+            }
         }
     }
 }
@@ -519,18 +544,25 @@ __global__ void ens_scale_efield(const RunDesc* __restrict__ runs, int nruns, ui
 }
 
 // Per-run energies of the step into hist[step*nruns + r]: field energy
-// 0.5*sum(Ex^2+Ey^2) and kinetic 0.5*m*sum(v^2), fixed partition per run.
-constexpr int EN_BLOCKS_PER_RUN = 32;
-__global__ void ens_energy_partials(const RunDesc* __restrict__ runs, const double* __restrict__ Ex,
+// 0.5*sum(Ex^2+Ey^2) (FP64) and kinetic 0.5*m*sum(vx^2+vy^2), summed in FP32
+// per thread (a few thousand particles) and in FP64 across threads (FP64
+// arithmetic per particle would cost more than the step's particle work). Blocks are given to runs in
+// proportion to their particles (EN_CHUNK per block); a run's blocks are added
+// in index order, so the result does not depend on the launch.
+constexpr size_t EN_CHUNK = 1 << 20;
+__global__ void ens_energy_partials(const RunDesc* __restrict__ runs, int nruns, const double* __restrict__ Ex,
                                     const double* __restrict__ Ey, const float* __restrict__ vx,
-                                    const float* __restrict__ vy, const float* __restrict__ mass,
-                                    double* __restrict__ partial) {
-    const int r = blockIdx.x / EN_BLOCKS_PER_RUN, b = blockIdx.x % EN_BLOCKS_PER_RUN;
-    const RunDesc& R = runs[r];
+                                    const float* __restrict__ vy, double* __restrict__ partial) {
+    __shared__ uint32_t ebase[MAX_RUNS];
     __shared__ double ws[2][ENS_THREADS / 32];
+    for (int i = threadIdx.x; i < nruns; i += ENS_THREADS) ebase[i] = runs[i].en_base;
+    __syncthreads();
+    const int r = find_run(ebase, nruns, blockIdx.x);
+    const RunDesc& R = runs[r];
+    const int b = (int)(blockIdx.x - R.en_base), nb = (int)R.en_blocks;
     double fe = 0.0, ke = 0.0;
     {
-        const size_t n = R.cells, chunk = (n + EN_BLOCKS_PER_RUN - 1) / EN_BLOCKS_PER_RUN;
+        const size_t n = R.cells, chunk = (n + nb - 1) / nb;
         const size_t s = (size_t)b * chunk, e = s + chunk < n ? s + chunk : n;
         for (size_t i = s + threadIdx.x; i < e; i += ENS_THREADS) {
             const double ex = Ex[R.cell_base + i], ey = Ey[R.cell_base + i];
@@ -538,13 +570,14 @@ __global__ void ens_energy_partials(const RunDesc* __restrict__ runs, const doub
         }
     }
     {
-        const size_t n = R.np, chunk = (n + EN_BLOCKS_PER_RUN - 1) / EN_BLOCKS_PER_RUN;
+        const size_t n = R.np, chunk = (n + nb - 1) / nb;
         const size_t s = (size_t)b * chunk, e = s + chunk < n ? s + chunk : n;
-        const double m = (double)mass[r];
+        float kf = 0.0f;
         for (size_t i = s + threadIdx.x; i < e; i += ENS_THREADS) {
-            const double a = vx[R.pbase + i], c = vy[R.pbase + i];
-            ke = __dadd_rn(ke, __dmul_rn(__dmul_rn(0.5, m), __dadd_rn(__dmul_rn(a, a), __dmul_rn(c, c))));
+            const float a = vx[R.pbase + i], c = vy[R.pbase + i];
+            kf += a * a + c * c;
         }
+        ke = (double)kf;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -568,18 +601,20 @@ __global__ void ens_energy_partials(const RunDesc* __restrict__ runs, const doub
     }
 }
 
-__global__ void ens_energy_final(const double* __restrict__ partial, int nruns, const int* __restrict__ step,
+__global__ void ens_energy_final(const RunDesc* __restrict__ runs, const float* __restrict__ mass,
+                                 const double* __restrict__ partial, int nruns, const int* __restrict__ step,
                                  int max_steps, double* __restrict__ fe_hist, double* __restrict__ ke_hist) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     const int s = *step;
     if (r < nruns && s < max_steps) {
+        const RunDesc& R = runs[r];
         double a = 0.0, c = 0.0;
-        for (int b = 0; b < EN_BLOCKS_PER_RUN; ++b) {
-            a = __dadd_rn(a, partial[2 * (r * EN_BLOCKS_PER_RUN + b)]);
-            c = __dadd_rn(c, partial[2 * (r * EN_BLOCKS_PER_RUN + b) + 1]);
+        for (uint32_t b = R.en_base; b < R.en_base + R.en_blocks; ++b) {
+            a = __dadd_rn(a, partial[2 * b]);
+            c = __dadd_rn(c, partial[2 * b + 1]);
         }
         fe_hist[(size_t)s * nruns + r] = __dmul_rn(0.5, a);
-        ke_hist[(size_t)s * nruns + r] = c;
+        ke_hist[(size_t)s * nruns + r] = __dmul_rn(__dmul_rn(0.5, (double)mass[r]), c);
     }
 }
 
@@ -609,6 +644,7 @@ struct pic_ens {
     int sort_interval = 0, use_graph = 1;
     long long steps_done = 0;
     int coop_blocks = 0;
+    uint32_t en_blocks = 0;  // blocks of the energy sums (all runs)
     bool tuned = false;
     // batched FFT per grid size
     struct Batch {
@@ -735,11 +771,11 @@ int poisson(pic_ens* e) {
 int energies(pic_ens* e) {
     pic_ctx* c = e->c;
     const int nr = (int)e->runs.size();
-    ens_energy_partials<<<nr * EN_BLOCKS_PER_RUN, ENS_THREADS, 0, c->stream>>>(e->druns, c->Ex, c->Ey, c->vx, c->vy,
-                                                                              e->dmass, e->en_partial);
+    ens_energy_partials<<<e->en_blocks, ENS_THREADS, 0, c->stream>>>(e->druns, nr, c->Ex, c->Ey, c->vx, c->vy,
+                                                                    e->en_partial);
     PIC_TRY(check_launch(c, "ens_energy_partials"));
-    ens_energy_final<<<(nr + 127) / 128, 128, 0, c->stream>>>(e->en_partial, nr, e->step_ctr, e->hist_cap, e->fe_hist,
-                                                              e->ke_hist);
+    ens_energy_final<<<(nr + 127) / 128, 128, 0, c->stream>>>(e->druns, e->dmass, e->en_partial, nr, e->step_ctr,
+                                                              e->hist_cap, e->fe_hist, e->ke_hist);
     PIC_TRY(check_launch(c, "ens_energy_final"));
     bump_step<<<1, 1, 0, c->stream>>>(e->step_ctr);
     c->launches += 3;
@@ -906,6 +942,11 @@ int pic_ens_create(const pic_ens_member* runs_in, int nruns, const pic_ens_confi
         pb += r.np;
     }
     c->n = n;
+    for (auto& r : e->runs) {
+        r.en_base = e->en_blocks;
+        r.en_blocks = (uint32_t)std::max<size_t>(1, (r.np + EN_CHUNK - 1) / EN_CHUNK);
+        e->en_blocks += r.en_blocks;
+    }
     int out_rc = PIC_OK;
     auto A = [&](size_t bytes) { return out_rc ? nullptr : dalloc(bytes, &out_rc); };
     e->druns = (RunDesc*)A(sizeof(RunDesc) * nruns);
@@ -913,7 +954,7 @@ int pic_ens_create(const pic_ens_member* runs_in, int nruns, const pic_ens_confi
     e->bar = (unsigned*)A(2 * sizeof(unsigned));
     e->err = (int*)A(sizeof(int));
     e->step_ctr = (int*)A(sizeof(int));
-    e->en_partial = (double*)A(sizeof(double) * 2 * nruns * EN_BLOCKS_PER_RUN);
+    e->en_partial = (double*)A(sizeof(double) * 2 * e->en_blocks);
     if (out_rc == PIC_OK) out_rc = ensure_fields(c);
     if (out_rc == PIC_OK) out_rc = upload_runs(e);
     if (out_rc == PIC_OK && (cudaMemcpyAsync(e->dmass, mass.data(), sizeof(float) * nruns, cudaMemcpyHostToDevice,

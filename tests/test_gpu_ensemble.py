@@ -61,7 +61,8 @@ def test_graph_and_sort_interval_change_nothing(pg):
         kb = np.lexsort((b["vy"], b["vx"], b["y"], b["x"]))
         for k in ("x", "y", "vx", "vy"):
             assert np.array_equal(a[k][ka], b[k][kb])
-    assert np.allclose(ke0, ke1, rtol=1e-12)
+    # kinetic energy is summed in FP32 per thread, so particle order moves its last bits
+    assert np.allclose(ke0, ke1, rtol=1e-6)
     assert all(w >= 1 and h >= 1 for w, h in tiles)
 
 
