@@ -229,6 +229,10 @@ typedef struct pic_run_config {
     double rbgs_tol;       /* poisson == 1: relative residual target */
     int rbgs_max_iters;    /* poisson == 1: sweep limit per solve */
     int rbgs_check_every;  /* poisson == 1: sweeps between residual checks */
+    int rbgs_warm;         /* poisson == 1: starting guess of each solve: 0 the previous step's phi;
+                              1 cubic extrapolation of the last three solutions; 2 extrapolation plus
+                              the trained network's correction (pic_gpu_ws_*). Modes 1 and 2 need
+                              pic_gpu_ws_init; until three solutions exist they start from phi. */
 } pic_run_config;
 /* Advances `steps` steps; history (steps entries, may be NULL) receives every
  * step's diagnostics (SimulationResult::*_history, simulation.hpp:49-60). */

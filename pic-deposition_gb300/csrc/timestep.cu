@@ -25,6 +25,8 @@ namespace picgb {
 
 int move(pic_ctx* c, double dt, bool gather, bool push);
 int rbgs_solve_async(pic_ctx* c, double tol, int max_iters, int check_every);
+int ws_warm_guess(pic_ctx* c, int mode);
+int ws_record_solution(pic_ctx* c);
 
 // pic_diag from the raw sums in red_out (same formulas as read_diagnostics).
 __global__ void finalize_diag(const double* __restrict__ r, double vol, double* __restrict__ hist,
@@ -48,8 +50,10 @@ __global__ void finalize_diag(const double* __restrict__ r, double vol, double* 
 }
 
 static int solve(pic_ctx* c, const pic_run_config* cfg) {
-    if (cfg->poisson == 1) return rbgs_solve_async(c, cfg->rbgs_tol, cfg->rbgs_max_iters, cfg->rbgs_check_every);
-    return poisson_fft(c);
+    if (cfg->poisson != 1) return poisson_fft(c);
+    if (cfg->rbgs_warm > 0) PIC_TRY(ws_warm_guess(c, cfg->rbgs_warm));
+    PIC_TRY(rbgs_solve_async(c, cfg->rbgs_tol, cfg->rbgs_max_iters, cfg->rbgs_check_every));
+    return cfg->rbgs_warm > 0 ? ws_record_solution(c) : PIC_OK;
 }
 
 // One step; `do_sort` selects the variant with the cell sort.
@@ -148,6 +152,10 @@ static int capture(pic_ctx* c, const pic_run_config* cfg, bool do_sort, double* 
 int run_steps(pic_ctx* c, const pic_run_config* cfg, int steps, pic_diag* history) {
     if (cfg->scheme < PIC_SCHEME_NGP || cfg->scheme > PIC_SCHEME_ESIRKEPOV) return fail(PIC_ERR_ARG, "unknown scheme");
     if (cfg->poisson != 0 && cfg->poisson != 1) return fail(PIC_ERR_ARG, "poisson must be 0 (FFT) or 1 (RBGS)");
+    if (cfg->poisson == 1 && (cfg->rbgs_warm < 0 || cfg->rbgs_warm > 2))
+        return fail(PIC_ERR_ARG, "rbgs_warm must be 0, 1 or 2");
+    if (cfg->poisson == 1 && cfg->rbgs_warm > 0 && !c->ws)
+        return fail(PIC_ERR_STATE, "rbgs_warm 1 and 2 need pic_gpu_ws_init");
     if (steps < 0) return fail(PIC_ERR_ARG, "steps < 0");
     if (steps == 0) return PIC_OK;
     int rc = PIC_OK;

@@ -377,6 +377,20 @@ int ws_set_phi(pic_ctx* c, const double* phi) {
 
 }  // namespace
 
+// Starting guess of a time-step solve (pic_run_config::rbgs_warm): mode 1 the
+// extrapolation, mode 2 extrapolation + network; the previous phi (already in
+// the context) until three solutions have been recorded.
+int ws_warm_guess(pic_ctx* c, int mode) {
+    if (!c->ws || c->ws->hist_n < 3 || mode <= 0) return PIC_OK;
+    PIC_TRY(rbgs_prepare(c));
+    return ws_guess(c, mode);
+}
+
+int ws_record_solution(pic_ctx* c) {
+    if (!c->ws) return PIC_OK;
+    return ws_push_history(c, c->phi);
+}
+
 void release_ws(pic_ctx* c) {
     WsState* s = c->ws;
     if (!s) return;

@@ -92,7 +92,7 @@ class RunConfig(C.Structure):
     """pic_run_config (include/pic_gb300.h)."""
     _fields_ = [("scheme", C.c_int), ("poisson", C.c_int), ("dt", C.c_double), ("background", C.c_double),
                 ("sort_interval", C.c_int), ("use_graph", C.c_int), ("rbgs_tol", C.c_double),
-                ("rbgs_max_iters", C.c_int), ("rbgs_check_every", C.c_int)]
+                ("rbgs_max_iters", C.c_int), ("rbgs_check_every", C.c_int), ("rbgs_warm", C.c_int)]
 
 
 _SIGS.append(("pic_gpu_run", [_vp, C.POINTER(RunConfig), C.c_int, C.POINTER(_Diag)]))
@@ -514,11 +514,11 @@ class Context:
                 "phi_diff": np.array([s.phi_diff for s in st])}
 
     def run(self, steps, scheme=1, dt=0.01, background=0.0, sort_interval=0, use_graph=False, poisson=0,
-            rbgs_tol=1e-8, rbgs_max_iters=100000, rbgs_check_every=64):
+            rbgs_tol=1e-8, rbgs_max_iters=100000, rbgs_check_every=64, rbgs_warm=0):
         """Advances `steps` time steps; returns the per-step diagnostics as a (steps, 6) array in
         pic_diag order (charge_error, total_charge, integrated_rho, kinetic, field, total)."""
         cfg = RunConfig(int(scheme), int(poisson), float(dt), float(background), int(sort_interval),
-                        int(use_graph), float(rbgs_tol), int(rbgs_max_iters), int(rbgs_check_every))
+                        int(use_graph), float(rbgs_tol), int(rbgs_max_iters), int(rbgs_check_every), int(rbgs_warm))
         hist = (_Diag * max(steps, 1))()
         _check(lib().pic_gpu_run(self.h, C.byref(cfg), int(steps), hist))
         return np.array([[getattr(h, k) for k, _ in _Diag._fields_] for h in hist[:steps]])

@@ -243,8 +243,9 @@ bool testLangmuirSimulation() {
         const auto r = sim.run();
         // The reference adds the neutralising background before its diagnostics
         // (simulation.cpp:52-59,111-117), so integratedRho is ~0 against a particle
-        // charge of -1 and the reported charge error of a Langmuir run is 1.
-        ok &= expectNear(r.final_charge_error, 1.0, 1e-10, "Simulation " + pic::schemeName(s) + " charge error");
+        // charge of -1 and the reported charge error of a Langmuir run is 1 (to the
+        // FP32 rounding of the stored charge -1/N, which sets sum|q|).
+        ok &= expectNear(r.final_charge_error, 1.0, 1e-6, "Simulation " + pic::schemeName(s) + " charge error");
         ok &= expectNear(std::isfinite(r.energy_drift) ? 0.0 : 1.0, 0.0, 0.0,
                          "Simulation " + pic::schemeName(s) + " finite energy");
         ok &= expectNear(r.energy_history.size(), 200.0, 0.0, "Simulation " + pic::schemeName(s) + " history length");

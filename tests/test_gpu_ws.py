@@ -73,3 +73,26 @@ def test_training_lowers_loss_and_solves_agree(pg):
     assert np.all(st["resid"] <= 1e-8)
     assert np.all(st["guess_resid"][:, 1] < st["guess_resid"][:, 0])
     assert np.all(st["phi_diff"] <= 1e-4 * np.sqrt(np.mean(phi ** 2)))
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_time_step_warm_start_keeps_the_answer(pg, mode):
+    """pic_gpu_run with a red-black Gauss-Seidel solve warm-started from the
+    extrapolation (1) or extrapolation + network (2) follows the same trajectory
+    as the previous-phi start (0): every solve reaches the same tolerance."""
+    nx, ny, ppc, dt = 128, 32, 16, 0.1
+    p = landau(nx, ny, ppc, seed=11)
+    n = len(p["x"])
+    bg = 1.0 / (nx * ny)
+    out = []
+    for m in (0, mode):
+        with pg.Context(nx, ny, float(nx), float(ny), n) as c:
+            c.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"])
+            c.ws_init(seed=2)
+            c.ws_generate(4, dt, bg, sort_interval=0)  # three solutions in the history
+            h = c.run(6, scheme=1, dt=dt, background=bg, poisson=1, rbgs_tol=1e-10, rbgs_max_iters=400000,
+                      rbgs_check_every=16, rbgs_warm=m)
+            out.append((h, c.fields()[0]))
+    (h0, phi0), (h1, phi1) = out
+    assert np.allclose(h0[:, 3:], h1[:, 3:], rtol=1e-7, atol=0)
+    assert np.max(np.abs(phi0 - phi1)) <= 1e-6 * np.max(np.abs(phi0))
