@@ -64,7 +64,7 @@ def test_main_test_program(exe):
     lines = r.stdout.splitlines()
     assert r.returncode == 0, r.stdout + r.stderr
     assert "FAIL" not in r.stderr
-    assert sum(ln.startswith("PASS") for ln in lines) >= 30, r.stdout
+    assert sum(ln.startswith("PASS") for ln in lines) >= 28, r.stdout
 
 
 @pytest.mark.gpu
