@@ -610,6 +610,8 @@ def run_gs_study(args):
     with pg.Context(GS_N, GS_N, float(GS_N), float(GS_N), n) as c:
         c.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"])
         del p
+        c.set_rbgs_precision(args.gs_mixed)
+        out["sweep_precision"] = "FP32 sweeps, FP64 refinement" if args.gs_mixed else "FP64"
         c.ws_init(seed=1, dataset_capacity=args.gs_pairs)
         t0 = time.time()
         out["pairs"] = c.ws_generate(args.gs_pairs + 3, GS_DT, bg, sort_interval=20)
@@ -664,6 +666,7 @@ def main():
     ap.add_argument("--gs-lr", type=float, default=1e-3)
     ap.add_argument("--gs-steps", type=int, default=8)
     ap.add_argument("--gs-check", type=int, default=16)
+    ap.add_argument("--gs-mixed", type=int, default=1, help="1: FP32 sweeps with FP64 refinement, 0: FP64 sweeps")
     args = ap.parse_args()
     PPC = args.ppc
     if args.warmup < 3:

@@ -203,6 +203,13 @@ int pic_gpu_poisson_fft(pic_ctx* ctx);
 int pic_gpu_poisson_rbgs(pic_ctx* ctx, double tol, int max_iters, int warm_start, int check_every, int* iters_out,
                          double* resid_out);
 
+/* Arithmetic of the red-black Gauss-Seidel sweeps (this context, all later solves):
+ * 0 (default) FP64 sweeps; 1 FP32 sweeps on a correction equation, refined in FP64
+ * (r = b - A phi in FP64, A e = r relaxed in FP32, phi += e, until the FP64
+ * relative residual meets tol). Both stop on the same FP64 test; mode 1 needs a
+ * grid that tiles into 64x32 (or smaller power-of-two) tiles, else it runs mode 0. */
+int pic_gpu_set_rbgs_precision(pic_ctx* ctx, int mixed);
+
 /* ---- particle motion ---- */
 
 /* pic::gatherFieldsSoA (src/deposition/deposition.cpp:335-356): v += -(q/m)*E*dt. */

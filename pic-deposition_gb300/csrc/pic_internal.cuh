@@ -100,6 +100,8 @@ struct pic_ctx {
     double *rb_b = nullptr, *rb_partial = nullptr, *rb_scalars = nullptr;
     double* rb_ps = nullptr;   // persistent solve: partial sums, barrier, results
     int rbgs_persistent = 1;   // use the one-launch solve where it applies
+    int rbgs_mixed = 0;        // FP32 sweeps on FP64-refined corrections (pic_gpu_set_rbgs_precision)
+    double* rb_mix = nullptr;  // mixed solve: FP64 residual, FP32 rhs and correction
     int last_rbgs_iters = 0;
     double last_rbgs_resid = 0.0, first_rbgs_resid = 0.0;
     // learned warm start (warmstart.cu)

@@ -406,9 +406,226 @@ static int rbgs_solve_persistent(pic_ctx* c, const RbArgs& a, double tol, int ma
     return PIC_OK;
 }
 
+// ---- mixed precision: FP32 sweeps on the correction, FP64 residual --------
+// Iterative refinement: r = b - A phi in FP64; A e = r is relaxed in FP32 by the
+// same red-black sweeps (one cooperative launch, 8-cell halo, 4 sweeps per grid
+// barrier) until ||r - A e|| <= itol ||r||; phi += e in FP64; repeat until the
+// FP64 relative residual meets tol. The answer meets the same FP64 test as the
+// FP64 solve; sweeps are counted over all corrections.
+constexpr int PF_HALO = 8;
+
+__global__ void rb_residual_field(RbArgs a, const double* __restrict__ phi, double* __restrict__ r);
+
+struct PsArgsF {
+    float* e;        // correction (in/out)
+    const float* r;  // right-hand side of the correction
+    int Nx, Ny;
+    float ix2, iy2, inv_denom, denom;
+    int tw, th, tiles_x, ew, eh;
+    float itol;
+    int max_sweeps, check_every;
+    double* partial;
+    unsigned* bar;
+    int* err;
+    double* out;  // [0] sweeps
+};
+
+__global__ void __launch_bounds__(PS_THREADS) rbgs_persistent_f32(PsArgsF p) {
+    extern __shared__ float pfm[];
+    const int E = p.ew * p.eh;
+    float* se = pfm;
+    float* sr = pfm + E;
+    __shared__ double tot[2];
+    const int tx = blockIdx.x % p.tiles_x, ty = blockIdx.x / p.tiles_x;
+    const int ox = tx * p.tw - PF_HALO, oy = ty * p.th - PF_HALO;
+    for (int i = threadIdx.x; i < E; i += PS_THREADS) {
+        const int ly = i / p.ew, lx = i - ly * p.ew;
+        const size_t g = (size_t)ps_wrap(oy + ly, p.Ny) * p.Nx + ps_wrap(ox + lx, p.Nx);
+        sr[i] = p.r[g];
+        se[i] = p.e[g];
+    }
+    __syncthreads();
+    const int nown = p.tw * p.th;
+    double rr0 = 0.0;
+    for (int t = threadIdx.x; t < nown; t += PS_THREADS) {
+        const int i = (PF_HALO + t / p.tw) * p.ew + PF_HALO + t % p.tw;
+        rr0 += (double)sr[i] * (double)sr[i];
+    }
+    rr0 = rb_block_sum(rr0);
+    if (threadIdx.x == 0) p.partial[2 * blockIdx.x + 1] = rr0;
+    int it = 0;
+    double prev = 1e300;
+    for (;;) {
+        if (it % p.check_every == 0 || it >= p.max_sweeps) {
+            double rr = 0.0;
+            for (int t = threadIdx.x; t < nown; t += PS_THREADS) {
+                const int i = (PF_HALO + t / p.tw) * p.ew + PF_HALO + t % p.tw;
+                const float ae = p.denom * se[i] - p.ix2 * (se[i - 1] + se[i + 1]) - p.iy2 * (se[i - p.ew] + se[i + p.ew]);
+                const double q = (double)(sr[i] - ae);
+                rr += q * q;
+            }
+            rr = rb_block_sum(rr);
+            if (threadIdx.x == 0) p.partial[2 * blockIdx.x] = rr;
+            if (!ps_barrier(p.bar, p.err)) break;
+            if (threadIdx.x == 0) {
+                double s1 = 0.0, s2 = 0.0;
+                for (unsigned k = 0; k < gridDim.x; ++k) {
+                    s1 += p.partial[2 * k];
+                    s2 += p.partial[2 * k + 1];
+                }
+                tot[0] = s1;
+                tot[1] = s2;
+            }
+            __syncthreads();
+            const double res = tot[1] > 0.0 ? sqrt(tot[0] / tot[1]) : 0.0;
+            // stop at the tolerance, the sweep limit, or when FP32 rounding stalls the residual
+            if (res <= (double)p.itol || it >= p.max_sweeps || res > 0.999 * prev) break;
+            prev = res;
+        }
+        for (int k = 0; k < PF_HALO; ++k) {
+            const int color = k & 1;
+            const int lo = k + 1;
+            const int rows = p.eh - 2 * lo, cols = p.ew - 2 * lo;
+            const int half = (cols + 1) >> 1;
+            for (int t = threadIdx.x; t < rows * half; t += PS_THREADS) {
+                const int rw = t / half, m = t - rw * half;
+                const int ly = lo + rw;
+                const int lx = lo + (((ox + lo + oy + ly) & 1) ^ color) + 2 * m;
+                if (lx >= p.ew - lo) continue;
+                const int i = ly * p.ew + lx;
+                se[i] = ((se[i - 1] + se[i + 1]) * p.ix2 + (se[i - p.ew] + se[i + p.ew]) * p.iy2 + sr[i]) * p.inv_denom;
+            }
+            __syncthreads();
+        }
+        it += PF_HALO / 2;
+        for (int t = threadIdx.x; t < nown; t += PS_THREADS) {
+            const int ly = PF_HALO + t / p.tw, lx = PF_HALO + t % p.tw;
+            p.e[(size_t)(oy + ly) * p.Nx + (ox + lx)] = se[ly * p.ew + lx];
+        }
+        if (!ps_barrier(p.bar, p.err)) break;
+        for (int i = threadIdx.x; i < E; i += PS_THREADS) {
+            const int ly = i / p.ew, lx = i - ly * p.ew;
+            if (ly >= PF_HALO && ly < PF_HALO + p.th && lx >= PF_HALO && lx < PF_HALO + p.tw) continue;
+            se[i] = p.e[(size_t)ps_wrap(oy + ly, p.Ny) * p.Nx + ps_wrap(ox + lx, p.Nx)];
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) p.out[0] = (double)it;
+}
+
+__global__ void rb_to_f32(const double* __restrict__ r, size_t n, float* __restrict__ r32, float* __restrict__ e) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        r32[i] = __double2float_rn(r[i]);
+        e[i] = 0.0f;
+    }
+}
+
+__global__ void rb_add_correction(double* __restrict__ phi, const float* __restrict__ e, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) phi[i] = __dadd_rn(phi[i], (double)e[i]);
+}
+
+// The mixed-precision solve; PIC_ERR_UNSUPPORTED (nothing queued) when the
+// grid does not tile evenly or the tiles cannot all be resident.
+static int rbgs_solve_mixed(pic_ctx* c, const RbArgs& a, double tol, int max_iters, int check_every, int* it_out,
+                            double* res_out) {
+    static const int cw[] = {64, 32, 16, 8, 4, 2};
+    static const int ch[] = {32, 16, 8, 4, 2};
+    const int tw = largest_divisor_tile(c->Nx, cw, 6), th = largest_divisor_tile(c->Ny, ch, 5);
+    if (!tw || !th) return PIC_ERR_UNSUPPORTED;
+    const int tiles_x = c->Nx / tw, blocks = tiles_x * (c->Ny / th);
+    const int ew = tw + 2 * PF_HALO, eh = th + 2 * PF_HALO;
+    const size_t smem = (size_t)2 * ew * eh * sizeof(float);
+    if (blocks > PS_MAX_BLOCKS || smem > 48 * 1024) return PIC_ERR_UNSUPPORTED;
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rbgs_persistent_f32, PS_THREADS, smem);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (per_sm * sms < blocks) return PIC_ERR_UNSUPPORTED;
+    int rc = PIC_OK;
+    if (!c->rb_ps) c->rb_ps = (double*)dalloc((2 * PS_MAX_BLOCKS + 8) * sizeof(double), &rc);
+    if (rc) return rc;
+    if (!c->rb_mix) c->rb_mix = (double*)dalloc(c->G * (8 + 4 + 4), &rc);
+    if (rc) return rc;
+    double* r64 = c->rb_mix;
+    float* r32 = reinterpret_cast<float*>(r64 + c->G);
+    float* e32 = r32 + c->G;
+    double* out = c->rb_ps + 2 * PS_MAX_BLOCKS;
+    unsigned* bar = reinterpret_cast<unsigned*>(out + 4);
+    int* err = reinterpret_cast<int*>(out + 5);
+    PIC_CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), c->stream));
+    PIC_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+    const unsigned gb = (unsigned)((c->G + 255) / 256);
+    const int ce = check_every < 4 ? 4 : (check_every / 4) * 4;
+    int it = 0;
+    double res = 0.0, prev_res = 0.0;
+    for (int outer = 0;; ++outer) {
+        PIC_TRY(rb_residual_async(c, a));
+        double s[3];
+        PIC_CUDA_TRY(cudaMemcpyAsync(s, c->rb_scalars, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
+        PIC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        res = s[2] > 0.0 ? std::sqrt(s[1] / s[2]) : std::sqrt(s[1]);
+        if (outer == 0) c->first_rbgs_resid = res;
+        if (res <= tol || it >= max_iters) break;
+        rb_residual_field<<<gb, 256, 0, c->stream>>>(a, c->phi, r64);
+        PIC_TRY(check_launch(c, "rb_residual_field"));
+        rb_to_f32<<<gb, 256, 0, c->stream>>>(r64, c->G, r32, e32);
+        PIC_TRY(check_launch(c, "rb_to_f32"));
+        // reduce the residual by what is left to reach tol; FP32 rounding of the
+        // correction limits one pass to about cond(A) * 2^-24 of the residual, so a
+        // pass aims at 1e-2 at most and the passes repeat
+        double itol = 0.5 * tol / res;
+        if (itol < 1e-2) itol = 1e-2;
+        if (itol > 0.5) itol = 0.5;
+        if (outer > 0 && res > 0.5 * prev_res) {  // a pass that no longer helps: finish in FP64
+            int it64 = 0;
+            double r64v = 0.0;
+            const double first = c->first_rbgs_resid;
+            const int prc = rbgs_solve_persistent(c, a, tol, (max_iters - it) & ~1, check_every & ~1 ? check_every & ~1 : 2,
+                                                  &it64, &r64v);
+            c->first_rbgs_resid = first;
+            if (prc == PIC_OK) {
+                it += it64;
+                res = r64v;
+                break;
+            }
+            if (prc != PIC_ERR_UNSUPPORTED) return prc;
+        }
+        prev_res = res;
+        PsArgsF p{e32, r32, c->Nx, c->Ny, (float)a.ix2, (float)a.iy2, (float)a.inv_denom, (float)a.denom,
+                  tw, th, tiles_x, ew, eh, (float)itol, max_iters - it, ce, c->rb_ps, bar, err, out};
+        cudaLaunchConfig_t lc{};
+        lc.gridDim = dim3(blocks);
+        lc.blockDim = dim3(PS_THREADS);
+        lc.dynamicSmemBytes = smem;
+        lc.stream = c->stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        lc.attrs = at;
+        lc.numAttrs = 1;
+        PIC_CUDA_TRY(cudaLaunchKernelEx(&lc, rbgs_persistent_f32, p));
+        c->launches += 3;
+        rb_add_correction<<<gb, 256, 0, c->stream>>>(c->phi, e32, c->G);
+        PIC_TRY(check_launch(c, "rb_add_correction"));
+        double h[6];
+        PIC_CUDA_TRY(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+        PIC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        int herr = 0;
+        std::memcpy(&herr, &h[5], sizeof(int));
+        if (herr) return fail(PIC_ERR_TIMEOUT, "red-black Gauss-Seidel: a grid-wide barrier timed out");
+        const int sw = (int)h[0];
+        it += sw > 0 ? sw : 1;  // a pass that made no sweep still counts, so the loop ends
+    }
+    *it_out = it;
+    *res_out = res;
+    return PIC_OK;
+}
+
 // Solves with the residual checked every `check_every` sweeps: in one
 // cooperative launch where possible, else one launch per colour with the
-// residual read on the host.
+// residual read on the host; with the mixed-precision option, FP32 sweeps on
+// FP64-refined corrections.
 int rbgs_solve(pic_ctx* c, double tol, int max_iters, int check_every, int* iters_out, double* resid_out) {
     if ((c->Nx & 1) || (c->Ny & 1)) return fail(PIC_ERR_UNSUPPORTED, "red-black Gauss-Seidel needs even Nx and Ny");
     if (max_iters < 0) return fail(PIC_ERR_ARG, "max_iters < 0");
@@ -419,8 +636,10 @@ int rbgs_solve(pic_ctx* c, double tol, int max_iters, int check_every, int* iter
     int it = 0;
     double res = 0.0;
     prof_begin(c, "rbgs");
-    const int prc = c->rbgs_persistent ? rbgs_solve_persistent(c, a, tol, max_iters, check_every, &it, &res)
-                                       : PIC_ERR_UNSUPPORTED;
+    int prc = PIC_ERR_UNSUPPORTED;
+    if (c->rbgs_mixed) prc = rbgs_solve_mixed(c, a, tol, max_iters, check_every, &it, &res);
+    if (prc == PIC_ERR_UNSUPPORTED && c->rbgs_persistent)
+        prc = rbgs_solve_persistent(c, a, tol, max_iters, check_every, &it, &res);
     if (prc != PIC_OK && prc != PIC_ERR_UNSUPPORTED) return prc;
     for (; prc == PIC_ERR_UNSUPPORTED;) {
         PIC_TRY(rb_residual_async(c, a));
@@ -480,6 +699,7 @@ int rbgs_solve_async(pic_ctx* c, double tol, int max_iters, int check_every) {
 }
 
 void release_rbgs(pic_ctx* c) {
+    dfree(c->rb_mix);
     dfree(c->rb_ps);
     dfree(c->rb_b);
     dfree(c->rb_partial);
@@ -489,6 +709,13 @@ void release_rbgs(pic_ctx* c) {
 }  // namespace picgb
 
 using namespace picgb;
+
+extern "C" int pic_gpu_set_rbgs_precision(pic_ctx* c, int mixed) {
+    if (!c) return fail(PIC_ERR_ARG, "NULL context");
+    if (mixed != 0 && mixed != 1) return fail(PIC_ERR_ARG, "precision must be 0 (FP64) or 1 (mixed)");
+    c->rbgs_mixed = mixed;
+    return PIC_OK;
+}
 
 extern "C" int pic_gpu_poisson_rbgs(pic_ctx* c, double tol, int max_iters, int warm_start, int check_every,
                                     int* iters_out, double* resid_out) {

@@ -158,6 +158,7 @@ class GenConfig(C.Structure):
 
 
 _SIGS.append(("pic_gpu_generate", [_vp, C.POINTER(GenConfig)]))
+_SIGS.append(("pic_gpu_set_rbgs_precision", [_vp, C.c_int]))
 
 
 class EnsMember(C.Structure):
@@ -443,6 +444,10 @@ class Context:
         ux, uy = C.c_double(), C.c_double()
         _check(lib().pic_gpu_get_current_fixed(self.h, _ptr(jx), _ptr(jy), C.byref(ux), C.byref(uy)))
         return jx, jy, ux.value, uy.value
+
+    def set_rbgs_precision(self, mixed: bool):
+        """False: FP64 sweeps; True: FP32 sweeps on FP64-refined corrections."""
+        _check(lib().pic_gpu_set_rbgs_precision(self.h, 1 if mixed else 0))
 
     def poisson_rbgs(self, tol=1e-8, max_iters=1_000_000, warm_start=True, check_every=64):
         it = C.c_int()

@@ -135,6 +135,25 @@ def test_rbgs_one_launch_equals_per_colour_launches(pg, nx, ny):
     assert np.array_equal(out[0][1], out[1][1])
 
 
+@pytest.mark.parametrize("nx,ny", [(512, 512), (64, 48)])
+def test_rbgs_mixed_precision_meets_the_same_fp64_test(pg, nx, ny):
+    """FP32 sweeps on FP64-refined corrections stop on the same FP64 relative
+    residual and give the FP64 solve's answer to within that tolerance."""
+    rng = np.random.default_rng(4)
+    rho = rng.normal(size=nx * ny)
+    out = []
+    for mixed in (False, True):
+        with pg.Context(nx, ny, float(nx), float(ny), 1) as c:
+            c.set_rho(rho)
+            c.set_rbgs_precision(mixed)
+            it, res = c.poisson_rbgs(tol=1e-10, max_iters=2_000_000, warm_start=False, check_every=16)
+            out.append((it, res, c.fields()[0]))
+    (it0, r0, p0), (it1, r1, p1) = out
+    assert r0 <= 1e-10 and r1 <= 1e-10
+    assert it1 <= 1.5 * it0 + 64
+    assert np.max(np.abs(p1 - p0)) <= 1e-6 * np.max(np.abs(p0))
+
+
 def test_rbgs_odd_grid_rejected(pg):
     with pg.Context(33, 32, 1.0, 1.0, 1) as c:
         c.set_rho(np.zeros(33 * 32))
