@@ -234,7 +234,8 @@ __global__ void __launch_bounds__(J_THREADS) deposit_current(JArgs a) {
             }
         }
         const uint32_t kprev = __shfl_up_sync(0xffffffffu, ckey, 1);
-        const unsigned H = __ballot_sync(0xffffffffu, lane == 0 || ckey != kprev);
+        // segments stop at lane 16: a run total covers <= 64 particles and fits int32
+        const unsigned H = __ballot_sync(0xffffffffu, lane == 0 || lane == 16 || ckey != kprev);
         const int segstart = 31 - __clz(H & upto);
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {

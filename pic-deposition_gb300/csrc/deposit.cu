@@ -11,24 +11,22 @@
 //    A - (sum of the others), so every particle deposits exactly A units and
 //    total charge is exact. Sums are int64, so the result does not depend on
 //    summation order: the tiled, atomic and oracle paths agree bit for bit.
-//    |value| <= 2^24 (+ a few units of remainder), so a warp-wide partial sum
-//    fits in int32.
-//  * Warp step (both fast paths). A warp handles 128 consecutive particles at
-//    a time: lane l takes particles 4l..4l+3, loaded with one 128-bit streaming
-//    load per field (each warp load is 512 contiguous bytes; the next step's
-//    loads are issued before this step's arithmetic). A lane sums its
-//    particles' stencil values in registers while they share a cell, then a
-//    segmented warp scan over the lanes' (cell, sums) leaves each run of equal
-//    cells' total in the run's last lane, which issues the atomics.
 //  * Sorted path (deposit_tiled). One CTA per tile of tile_w x tile_h cells;
-//    its int64 accumulators (tile + halo of 1 cell below, 2 above) live in
-//    shared memory. Warp w walks rows w, w+8, ... of the tile; the particles of
-//    one row of the tile are one contiguous run of the cell-sorted stream,
-//    [offsets[c0], offsets[c0+tile_w]). Run totals go to shared memory; at the
-//    end the tile is flushed to the global int64 grid once.
-//  * Any-order path (deposit_runs): the same warp step over the whole array,
-//    run totals straight to the global int64 grid (L2-resident). Needs no
-//    offsets; fast when particles are nearly cell-ordered (between sorts).
+//    the particles of one row of the tile are one contiguous run of the
+//    cell-sorted stream, staged into shared memory with cp.async; each lane
+//    sums 8 consecutive particles per stage in registers while they share a
+//    cell and adds the run totals to the tile's accumulators in shared memory
+//    (split into two native 32-bit atomics); at the end the tile is flushed to
+//    the global int64 grid once. Details at the kernel.
+//  * Any-order path (deposit_runs): a warp handles 128 consecutive particles
+//    at a time, lane l taking particles 4l..4l+3 (one 128-bit streaming load
+//    per field, the next step's loads issued first); a lane sums its
+//    particles' values while they share a cell, then a segmented warp scan over
+//    the lanes' (cell, sums) leaves each run's total in the run's last lane,
+//    which adds it to the global int64 grid (L2-resident). Needs no offsets;
+//    fast when particles are nearly cell-ordered (between sorts). The scan's
+//    segments stop at lane 16, so a run total covers at most 64 particles and
+//    fits int32 (|value| <= 2^24 + 3 per particle and entry).
 //  * Naive path (deposit_atomic): one thread per particle, one int64 atomic
 //    per stencil node into the global grid.
 //
@@ -353,115 +351,6 @@ __device__ __forceinline__ void load_quad(const DepArgs& a, uint32_t p0, bool ok
 __device__ __forceinline__ uint32_t u4(const uint4& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
 __device__ __forceinline__ float f4(const float4& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
 
-// Sorted path. See the file header: one CTA per tile, one warp per tile row at
-// a time; each warp step covers 128 particles (4 consecutive per lane, loaded
-// with one 128-bit load per field, the next step's loads issued before this
-// step's arithmetic). A lane sums its particles' stencil values in registers
-// while they share a cell (writing to shared memory only when its cell
-// changes); then a segmented warp scan over the lanes' (cell, sums) leaves each
-// run of equal cells' total in the run's last lane, which adds it to the tile's
-// shared int64 accumulators. The scan is correct for any order of cells; the
-// sortedness only makes runs long.
-template <int S>
-__global__ void __launch_bounds__(DEP_THREADS) deposit_tiled(DepArgs a) {
-    constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
-    constexpr int NV = NX * NX;
-    extern __shared__ long long sacc[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int SW = a.tile_w + 3;
-    const int tx = blockIdx.x % a.tiles_x, ty = blockIdx.x / a.tiles_x;
-    const int x0 = tx * a.tile_w, y0 = ty * a.tile_h;
-    const int tw = min(a.tile_w, a.Nx - x0), th = min(a.tile_h, a.Ny - y0);
-    const int nloc = (th + 3) * SW;
-    for (int i = threadIdx.x; i < nloc; i += DEP_THREADS) sacc[i] = 0;
-    __syncthreads();
-    const unsigned upto = (lane == 31) ? FULL : ((2u << lane) - 1u);
-    for (int r = warp; r < th; r += DEP_WARPS) {
-        const int iy = y0 + r;
-        const uint32_t rowbase = (uint32_t)iy * (uint32_t)a.Nx;
-        const uint32_t c0 = rowbase + (uint32_t)x0;
-        const uint32_t pbeg = a.offsets[c0], pend = a.offsets[c0 + tw];
-        const int lrow = r + 1 + LO;               // local row of frame row 0
-        const int lcol = 1 + LO - x0;              // local column of frame column 0 is ix + lcol
-        uint32_t base = pbeg & ~3u;
-        Quad<S> cur, nxt;
-        load_quad<S>(a, base + 4u * lane, base + 4u * lane < pend, cur);
-        while (base < pend) {
-            const uint32_t nbase = base + 128u;
-            if (nbase < pend) load_quad<S>(a, nbase + 4u * lane, nbase + 4u * lane < pend, nxt);
-            uint32_t ckey = NO_CELL;
-            int acc[NV];
-#pragma unroll
-            for (int k = 0; k < NV; ++k) acc[k] = 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const uint32_t p = base + 4u * lane + (uint32_t)k;
-                if (p >= pbeg && p < pend) {
-                    const uint32_t key = u4(cur.cell, k);
-                    if (key - c0 >= (uint32_t)tw) {
-                        set_dev_error(a.st, DEV_UNSORTED, p);
-                        continue;
-                    }
-                    int val[V];
-                    float vxx = 0.0f, vyy = 0.0f;
-                    if constexpr (S == S_ESK) {
-                        vxx = f4(cur.vx, k);
-                        vyy = f4(cur.vy, k);
-                    }
-                    if (!stencil_values<S>(a, f4(cur.xr, k), f4(cur.yr, k), f4(cur.q, k), vxx, vyy,
-                                           (int)(key - rowbase), iy, p, val))
-                        continue;
-                    if (key != ckey) {
-                        if (ckey != NO_CELL) {
-                            const int lx = (int)(ckey - rowbase) + lcol;
-#pragma unroll
-                            for (int q = 0; q < NV; ++q)
-                                if (acc[q] != 0) sadd(sacc, (lrow + q / NX) * SW + lx + (q % NX), acc[q]);
-                        }
-                        ckey = key;
-#pragma unroll
-                        for (int q = 0; q < NV; ++q) acc[q] = val[q];
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < NV; ++q) acc[q] += val[q];
-                    }
-                }
-            }
-            // segmented inclusive scan over lanes: runs of equal ckey
-            const uint32_t kprev = __shfl_up_sync(FULL, ckey, 1);
-            const unsigned H = __ballot_sync(FULL, lane == 0 || ckey != kprev);
-            const int segstart = 31 - __clz(H & upto);
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const bool take = lane - d >= segstart;
-#pragma unroll
-                for (int q = 0; q < NV; ++q) {
-                    const int o = __shfl_up_sync(FULL, acc[q], d);
-                    if (take) acc[q] += o;
-                }
-            }
-            const bool tail = (lane == 31) || ((H >> (lane + 1)) & 1u);
-            if (tail && ckey != NO_CELL) {
-                const int lx = (int)(ckey - rowbase) + lcol;
-#pragma unroll
-                for (int q = 0; q < NV; ++q)
-                    if (acc[q] != 0) sadd(sacc, (lrow + q / NX) * SW + lx + (q % NX), acc[q]);
-            }
-            cur = nxt;
-            base = nbase;
-        }
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nloc; i += DEP_THREADS) {
-        const long long v = sacc[i];
-        if (v != 0) {
-            const int ly = i / SW, lx = i % SW;
-            const int gx = wrap_i(x0 - 1 + lx, a.Nx), gy = wrap_i(y0 - 1 + ly, a.Ny);
-            atomicAdd(a.acc + (size_t)gy * a.Nx + gx, (unsigned long long)v);
-        }
-    }
-}
-
 // Adds a lane's sums for cell `key` straight to the global grid.
 template <int S>
 __device__ __forceinline__ void flush_global(const DepArgs& a, uint32_t key, const int (&acc)[Frame<S>::NX * Frame<S>::NX]) {
@@ -534,7 +423,9 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs(DepArgs a) {
             }
         }
         const uint32_t kprev = __shfl_up_sync(FULL, ckey, 1);
-        const unsigned H = __ballot_sync(FULL, lane == 0 || ckey != kprev);
+        // a segment never spans lanes 15|16: a run total covers at most 64
+        // particles, |total| <= 64 * (2^24 + 3) < 2^31
+        const unsigned H = __ballot_sync(FULL, lane == 0 || lane == 16 || ckey != kprev);
         const int segstart = 31 - __clz(H & upto);
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -597,43 +488,104 @@ constexpr uint32_t TSC_MAGIC_BITS = 0x4B400000u;
 
 __host__ __device__ constexpr bool tsc_central(int k) { return ((k >> 2) == 1 || (k >> 2) == 2) && ((k & 3) == 1 || (k & 3) == 2); }
 
-__device__ __forceinline__ void tsc_axis(float r, float (&X)[4], int& kmax) {
-    const bool s = r >= 0.5f;
-    const float t = s ? r - 1.0f : r;
-    const float dl = 0.5f - t, dr = 0.5f + t;
-    const float L = 0.5f * (dl * dl), Cw = 0.75f - t * t, R = 0.5f * (dr * dr);
-    X[0] = s ? 0.0f : L;
-    X[1] = s ? L : Cw;
-    X[2] = s ? Cw : R;
-    X[3] = s ? R : 0.0f;
-    kmax = X[2] > X[1] ? 2 : 1;
+// Paired FP32 arithmetic (two lanes of a 64-bit register, each IEEE
+// round-to-nearest like the scalar instruction): the x and y axes, or two
+// frame entries, in one instruction. A paired multiply is never followed by a
+// paired add or subtract of its result: the assembler fuses such a pair into
+// one multiply-add (one rounding) even with explicit .rn, which would change
+// the bits; those adds are scalar (add.rn.f32, never contracted).
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_pack(float lo, float hi) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f32x2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
 }
 
 // Frame values: central entries exact, the others biased by TSC_MAGIC_BITS.
-__device__ __forceinline__ void tsc_values(float rx, float ry, float qn, uint32_t (&val)[16]) {
+// Both axes' weights are computed as pairs (x, y) and the products of a frame
+// row as pairs of columns.
+__device__ __forceinline__ void tsc_accumulate(float rx, float ry, float qn, uint32_t (&acc)[16]) {
     const float aq = qn * 16777216.0f;
     const int A = __float2int_rn(aq);
-    float X[4], Y[4];
-    int kx, ky;
-    tsc_axis(rx, X, kx);
-    tsc_axis(ry, Y, ky);
+    const bool sx = rx >= 0.5f, sy = ry >= 0.5f;
+    float mx, my;
+    f2_unpack(f2_add(f2_pack(rx, ry), f2_pack(-1.0f, -1.0f)), mx, my);
+    const f32x2 t = f2_pack(sx ? mx : rx, sy ? my : ry);
+    const f32x2 half = f2_pack(0.5f, 0.5f);
+    const f32x2 dl = f2_sub(half, t), dr = f2_add(half, t);
+    const f32x2 L2 = f2_mul(half, f2_mul(dl, dl));
+    float ttx, tty;
+    f2_unpack(f2_mul(t, t), ttx, tty);
+    const f32x2 C2 = f2_pack(0.75f - ttx, 0.75f - tty);
+    const f32x2 R2 = f2_mul(half, f2_mul(dr, dr));
+    float Lx, Ly, Cx, Cy, Rx, Ry;
+    f2_unpack(L2, Lx, Ly);
+    f2_unpack(C2, Cx, Cy);
+    f2_unpack(R2, Rx, Ry);
+    const float X0 = sx ? 0.0f : Lx, X1 = sx ? Lx : Cx, X2 = sx ? Cx : Rx, X3 = sx ? Rx : 0.0f;
+    const float Y0 = sy ? 0.0f : Ly, Y1 = sy ? Ly : Cy, Y2 = sy ? Cy : Ry, Y3 = sy ? Ry : 0.0f;
+    const int kx = X2 > X1 ? 2 : 1, ky = Y2 > Y1 ? 2 : 1;
+    const f32x2 aq2 = f2_pack(aq, aq);
+    float ay[4];
+    f2_unpack(f2_mul(aq2, f2_pack(Y0, Y1)), ay[0], ay[1]);
+    f2_unpack(f2_mul(aq2, f2_pack(Y2, Y3)), ay[2], ay[3]);
+    const f32x2 x01 = f2_pack(X0, X1), x23 = f2_pack(X2, X3);
     uint32_t sum = 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        const float ay = aq * Y[j];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const float p = ay * X[i];
-            const uint32_t v = tsc_central(j * 4 + i) ? (uint32_t)__float2int_rn(p) : __float_as_uint(p + TSC_MAGIC);
-            val[j * 4 + i] = v;
-            sum += v;
+        const f32x2 ayj = f2_pack(ay[j], ay[j]);
+        const f32x2 p01 = f2_mul(ayj, x01), p23 = f2_mul(ayj, x23);
+        float v0, v1, v2, v3;
+        f2_unpack(p01, v0, v1);
+        f2_unpack(p23, v2, v3);
+        uint32_t e0, e1, e2, e3;
+        if (j == 0 || j == 3) {
+            e0 = __float_as_uint(v0 + TSC_MAGIC);
+            e1 = __float_as_uint(v1 + TSC_MAGIC);
+            e2 = __float_as_uint(v2 + TSC_MAGIC);
+            e3 = __float_as_uint(v3 + TSC_MAGIC);
+        } else {
+            e0 = __float_as_uint(v0 + TSC_MAGIC);
+            e1 = (uint32_t)__float2int_rn(v1);
+            e2 = (uint32_t)__float2int_rn(v2);
+            e3 = __float_as_uint(v3 + TSC_MAGIC);
         }
+        acc[j * 4 + 0] += e0;
+        acc[j * 4 + 1] += e1;
+        acc[j * 4 + 2] += e2;
+        acc[j * 4 + 3] += e3;
+        sum += e0 + e1 + e2 + e3;
     }
     const uint32_t rem = (uint32_t)A - (sum - 12u * TSC_MAGIC_BITS);
-    val[5] += (ky == 1 && kx == 1) ? rem : 0u;
-    val[6] += (ky == 1 && kx == 2) ? rem : 0u;
-    val[9] += (ky == 2 && kx == 1) ? rem : 0u;
-    val[10] += (ky == 2 && kx == 2) ? rem : 0u;
+    acc[5] += (ky == 1 && kx == 1) ? rem : 0u;
+    acc[6] += (ky == 1 && kx == 2) ? rem : 0u;
+    acc[9] += (ky == 2 && kx == 1) ? rem : 0u;
+    acc[10] += (ky == 2 && kx == 2) ? rem : 0u;
+}
+
+// One particle's frame values (tsc_accumulate into zeros).
+__device__ __forceinline__ void tsc_values(float rx, float ry, float qn, uint32_t (&val)[16]) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) val[q] = 0;
+    tsc_accumulate(rx, ry, qn, val);
 }
 
 // True total of entry q of a run of `cnt` particles.
@@ -641,95 +593,274 @@ __device__ __forceinline__ int tsc_true(int q, uint32_t acc, uint32_t cnt) {
     return tsc_central(q) ? (int)acc : (int)(acc - cnt * TSC_MAGIC_BITS);
 }
 
-// Sorted path for TSC (deposit_tiled with the values above).
-__global__ void __launch_bounds__(DEP_THREADS) deposit_tiled_tsc(DepArgs a) {
-    extern __shared__ long long sacc[];
+// Sorted path. One CTA of NW warps per tile of tile_w x tile_h cells. The
+// particles of one row of the tile are the contiguous slice
+// [offsets[c0], offsets[c0+tile_w]) of the cell-sorted stream; warp w walks
+// rows w, w+NW, ... and cuts each slice (from its 16-byte-aligned start) into
+// stages of 32*LPP consecutive particles.
+//  * Staging: a stage's fields are copied global -> shared with cp.async
+//    (16 bytes per lane and copy, each warp copy 512 contiguous bytes), two
+//    stage buffers per warp, the next stage in flight while this one is used.
+//    Quad Q (particles 4Q..4Q+3) of a field sits at slot Q ^ ((Q>>3)&(LPP/4-1)),
+//    which makes both the copies and the lanes' 128-bit reads conflict-free.
+//  * Lane chunks: lane l owns particles LPP*l .. LPP*l+LPP-1 of the stage and
+//    sums the values of the run of equal cells it is in, in 16 (TSC) or 4
+//    (CIC, NGP) registers; when its cell changes, the finished run moves to
+//    the lane's slots in shared memory (written out when a third run starts),
+//    and at the end of the chunk both runs are written out. No warp-wide
+//    scan; lanes are idle only at the ends of a slice. |value| <= 2^24 + 3 per
+//    particle and entry, so a run of LPP <= 16 particles fits in int32.
+//  * Tile accumulators: 64-bit shared atomics are not native (they compile to
+//    compare-and-swap loops), so a run total v is added as two native 32-bit
+//    shared atomics, v & (2^15-1) to an unsigned low word and v >> 15 to a
+//    signed high word; the node's total is hi * 2^15 + lo. A node receives at
+//    most one addition per run, and a run holds at least one particle of the
+//    tile, so both words stay exact while the tile holds fewer than 2^17
+//    particles (|v| < 2^29). Denser tiles add their runs straight to the
+//    global int64 grid.
+// At the end the tile is added to the global int64 grid once.
+template <int S>
+struct StageFields {
+    static constexpr int NF = (S == S_ESK) ? 6 : 4;  // cell, xr, yr, q (, vx, vy)
+};
+
+constexpr int TILE_SPLIT = 15;
+constexpr uint32_t TILE_SPLIT_MAX = 1u << 17;  // particles per tile for the split accumulators
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+template <int LPP>
+__device__ __forceinline__ int stage_slot(int Q) {
+    return Q ^ ((Q >> 3) & (LPP / 4 - 1));
+}
+
+// per warp: two stage buffers, then the lanes' previous-run sums ([entry][lane])
+template <int S, int LPP, int NW>
+__host__ __device__ constexpr size_t tiled_stage_bytes() {
+    return (size_t)NW * (2 * StageFields<S>::NF * (32 * LPP) * 4 + 32 * 4 * Frame<S>::NX * Frame<S>::NX);
+}
+
+template <int S, int LPP, int NW, int MINB>
+__global__ void __launch_bounds__(NW * 32, MINB) deposit_tiled(DepArgs a) {
+    constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
+    constexpr int NV = NX * NX;
+    constexpr int NF = StageFields<S>::NF;
+    constexpr int QL = LPP / 4;          // quads per lane per stage
+    constexpr int STAGE = 32 * LPP;      // particles per stage
+    constexpr int FB = STAGE * 4;        // bytes per field per stage buffer
+    constexpr int WB = 2 * NF * FB + 32 * 4 * NV;  // shared bytes per warp
+    static_assert(LPP % 4 == 0 && LPP <= 16, "a lane's run of LPP particles must fit in int32");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t s_count;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int SW = a.tile_w + 3;
     const int tx = blockIdx.x % a.tiles_x, ty = blockIdx.x / a.tiles_x;
     const int x0 = tx * a.tile_w, y0 = ty * a.tile_h;
     const int tw = min(a.tile_w, a.Nx - x0), th = min(a.tile_h, a.Ny - y0);
     const int nloc = (th + 3) * SW;
-    for (int i = threadIdx.x; i < nloc; i += DEP_THREADS) sacc[i] = 0;
+    uint32_t* slo = reinterpret_cast<uint32_t*>(smem_raw + tiled_stage_bytes<S, LPP, NW>());
+    int* shi = reinterpret_cast<int*>(slo + nloc);
+    const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(smem_raw) + (uint32_t)(warp * WB);
+    uint32_t* prv = reinterpret_cast<uint32_t*>(smem_raw + (size_t)warp * WB + 2 * NF * FB) + lane;
+    if (threadIdx.x == 0) s_count = 0;
+    for (int i = threadIdx.x; i < nloc; i += NW * 32) {
+        slo[i] = 0;
+        shi[i] = 0;
+    }
     __syncthreads();
-    const unsigned upto = (lane == 31) ? FULL : ((2u << lane) - 1u);
-    for (int r = warp; r < th; r += DEP_WARPS) {
+    if (threadIdx.x < th) {
+        const uint32_t c0 = (uint32_t)(y0 + threadIdx.x) * (uint32_t)a.Nx + (uint32_t)x0;
+        atomicAdd(&s_count, a.offsets[c0 + tw] - a.offsets[c0]);
+    }
+    __syncthreads();
+    const bool dense = s_count >= TILE_SPLIT_MAX;
+
+    const void* fptr[NF];
+    fptr[0] = a.cell;
+    fptr[1] = a.xr;
+    fptr[2] = a.yr;
+    fptr[3] = a.q;
+    if constexpr (NF == 6) {
+        fptr[4] = a.vx;
+        fptr[5] = a.vy;
+    }
+    // tile row r: first particle, end, aligned start, stages
+    struct Slice {
+        uint32_t pbeg, pend, base, nst;
+    };
+    auto slice = [&](int r) {
+        Slice sl;
+        const uint32_t c0 = (uint32_t)(y0 + r) * (uint32_t)a.Nx + (uint32_t)x0;
+        sl.pbeg = a.offsets[c0];
+        sl.pend = a.offsets[c0 + tw];
+        sl.base = sl.pbeg & ~3u;
+        sl.nst = sl.pend > sl.pbeg ? (sl.pend - sl.base + STAGE - 1) / STAGE : 0u;
+        return sl;
+    };
+    auto issue = [&](const Slice& sl, uint32_t t, int buf) {
+        const uint32_t dst = stage0 + (uint32_t)(buf * NF * FB);
+        const uint32_t sbase = sl.base + t * STAGE;
+#pragma unroll
+        for (int k = 0; k < QL; ++k) {
+            const int Q = k * 32 + lane;
+            const uint32_t p = sbase + 4u * (uint32_t)Q;
+            if (p < sl.pend) {
+#pragma unroll
+                for (int f = 0; f < NF; ++f)
+                    cp_async16(dst + (uint32_t)(f * FB + stage_slot<LPP>(Q) * 16),
+                               static_cast<const uint32_t*>(fptr[f]) + p);
+            }
+        }
+        cp_async_commit();
+    };
+
+    int r = warp;
+    Slice cs{0u, 0u, 0u, 0u};
+    while (r < th) {
+        cs = slice(r);
+        if (cs.nst) break;
+        r += NW;
+    }
+    if (r < th) issue(cs, 0u, 0);
+    uint32_t t = 0;
+    int buf = 0;
+    while (r < th) {
+        // the stage after this one: next stage of this row or first of the next non-empty row
+        int rn = r;
+        uint32_t tn = t + 1;
+        Slice ns = cs;
+        if (tn >= cs.nst) {
+            tn = 0;
+            ns.nst = 0;
+            for (rn = r + NW; rn < th; rn += NW) {
+                ns = slice(rn);
+                if (ns.nst) break;
+            }
+        }
+        if (rn < th) {
+            issue(ns, tn, buf ^ 1);
+        } else {
+            cp_async_commit();
+        }
+        cp_async_wait_1();
+        __syncwarp();
+
         const int iy = y0 + r;
         const uint32_t rowbase = (uint32_t)iy * (uint32_t)a.Nx;
         const uint32_t c0 = rowbase + (uint32_t)x0;
-        const uint32_t pbeg = a.offsets[c0], pend = a.offsets[c0 + tw];
-        const int lcol = -x0;  // local column of frame column 0 is ix + lcol (frame starts at ix - 1, halo 1)
-        uint32_t base = pbeg & ~3u;
-        Quad<S_TSC> cur, nxt;
-        load_quad<S_TSC>(a, base + 4u * lane, base + 4u * lane < pend, cur);
-        while (base < pend) {
-            const uint32_t nbase = base + 128u;
-            if (nbase < pend) load_quad<S_TSC>(a, nbase + 4u * lane, nbase + 4u * lane < pend, nxt);
-            uint32_t ckey = NO_CELL, cnt = 0;
-            uint32_t acc[16];
+        const int lrow = r + 1 + LO;   // local row of frame row 0
+        const int lcol = 1 + LO - x0;  // local column of frame column 0 is ix + lcol
+        const unsigned char* sb = smem_raw + (size_t)warp * WB + (size_t)buf * NF * FB;
+        // this lane's particles in this stage: [vbeg, vbeg + vlen) of the stream
+        const uint32_t cstart = cs.base + t * STAGE + (uint32_t)(LPP * lane);
+        const uint32_t vbeg = max(cstart, cs.pbeg), vend = min(cstart + LPP, cs.pend);
+        const uint32_t vlen = vend > vbeg ? vend - vbeg : 0u;
+        uint32_t ckey = NO_CELL, cnt = 0, pkey = NO_CELL, pcnt = 0;
+        uint32_t acc[NV];
 #pragma unroll
-            for (int k = 0; k < 16; ++k) acc[k] = 0;
+        for (int q = 0; q < NV; ++q) acc[q] = 0;
+        // writes out a run: sums in registers (acc) or in the lane's shared slots (prv)
+        auto flush = [&](bool from_prv, uint32_t key, uint32_t n) {
+            if (dense) {
+                int tv[NV];
+#pragma unroll
+                for (int q = 0; q < NV; ++q) {
+                    const uint32_t v = from_prv ? prv[32 * q] : acc[q];
+                    if constexpr (S == S_TSC)
+                        tv[q] = tsc_true(q, v, n);
+                    else
+                        tv[q] = (int)v;
+                }
+                flush_global<S>(a, key, tv);
+                return;
+            }
+            const int lx = (int)(key - rowbase) + lcol;
+#pragma unroll
+            for (int q = 0; q < NV; ++q) {
+                const uint32_t v = from_prv ? prv[32 * q] : acc[q];
+                int x;
+                if constexpr (S == S_TSC)
+                    x = tsc_true(q, v, n);
+                else
+                    x = (int)v;
+                if (x != 0) {
+                    const int i = (lrow + q / NX) * SW + lx + (q % NX);
+                    atomicAdd(slo + i, (uint32_t)x & ((1u << TILE_SPLIT) - 1u));
+                    atomicAdd(shi + i, x >> TILE_SPLIT);
+                }
+            }
+        };
+#pragma unroll
+        for (int h = 0; h < QL; ++h) {
+            const int Q = QL * lane + h;
+            const int off = stage_slot<LPP>(Q) * 16;
+            Quad<S> d;
+            d.cell = *reinterpret_cast<const uint4*>(sb + 0 * FB + off);
+            d.xr = *reinterpret_cast<const float4*>(sb + 1 * FB + off);
+            d.yr = *reinterpret_cast<const float4*>(sb + 2 * FB + off);
+            d.q = *reinterpret_cast<const float4*>(sb + 3 * FB + off);
+            if constexpr (NF == 6) {
+                d.vx = *reinterpret_cast<const float4*>(sb + 4 * FB + off);
+                d.vy = *reinterpret_cast<const float4*>(sb + 5 * FB + off);
+            }
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const uint32_t p = base + 4u * lane + (uint32_t)k;
-                if (p >= pbeg && p < pend) {
-                    const uint32_t key = u4(cur.cell, k);
+                const uint32_t p = cstart + (uint32_t)(4 * h + k);
+                if (p - vbeg < vlen) {
+                    const uint32_t key = u4(d.cell, k);
                     if (key - c0 >= (uint32_t)tw) {
                         set_dev_error(a.st, DEV_UNSORTED, p);
                         continue;
                     }
-                    uint32_t val[16];
-                    tsc_values(f4(cur.xr, k), f4(cur.yr, k), f4(cur.q, k), val);
-                    if (key != ckey) {
+                    if (key != ckey) {  // a new run: divergent only at cell boundaries
                         if (ckey != NO_CELL) {
-                            const int lx = (int)(ckey - rowbase) + lcol;
+                            if (pkey != NO_CELL) flush(true, pkey, pcnt);
 #pragma unroll
-                            for (int q = 0; q < 16; ++q) {
-                                const int v = tsc_true(q, acc[q], cnt);
-                                if (v != 0) sadd(sacc, (r + q / 4) * SW + lx + (q % 4), v);
+                            for (int q = 0; q < NV; ++q) {
+                                prv[32 * q] = acc[q];
+                                acc[q] = 0;
                             }
+                            pkey = ckey;
+                            pcnt = cnt;
+                            cnt = 0;
                         }
                         ckey = key;
-                        cnt = 1;
-#pragma unroll
-                        for (int q = 0; q < 16; ++q) acc[q] = val[q];
-                    } else {
-                        ++cnt;
-#pragma unroll
-                        for (int q = 0; q < 16; ++q) acc[q] += val[q];
                     }
+                    if constexpr (S == S_TSC) {
+                        tsc_accumulate(f4(d.xr, k), f4(d.yr, k), f4(d.q, k), acc);
+                    } else {
+                        int iv[V];
+                        float vxx = 0.0f, vyy = 0.0f;
+                        if constexpr (S == S_ESK) {
+                            vxx = f4(d.vx, k);
+                            vyy = f4(d.vy, k);
+                        }
+                        if (!stencil_values<S>(a, f4(d.xr, k), f4(d.yr, k), f4(d.q, k), vxx, vyy,
+                                               (int)(key - rowbase), iy, p, iv))
+                            continue;  // deposited by the general trajectory path
+#pragma unroll
+                        for (int q = 0; q < NV; ++q) acc[q] += (uint32_t)iv[q];
+                    }
+                    ++cnt;
                 }
             }
-            const uint32_t kprev = __shfl_up_sync(FULL, ckey, 1);
-            const unsigned H = __ballot_sync(FULL, lane == 0 || ckey != kprev);
-            const int segstart = 31 - __clz(H & upto);
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const bool take = lane - d >= segstart;
-                const uint32_t oc = __shfl_up_sync(FULL, cnt, d);
-                if (take) cnt += oc;
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const uint32_t o = __shfl_up_sync(FULL, acc[q], d);
-                    if (take) acc[q] += o;
-                }
-            }
-            const bool tail = (lane == 31) || ((H >> (lane + 1)) & 1u);
-            if (tail && ckey != NO_CELL) {
-                const int lx = (int)(ckey - rowbase) + lcol;
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const int v = tsc_true(q, acc[q], cnt);
-                    if (v != 0) sadd(sacc, (r + q / 4) * SW + lx + (q % 4), v);
-                }
-            }
-            cur = nxt;
-            base = nbase;
         }
+        if (ckey != NO_CELL) flush(false, ckey, cnt);
+        if (pkey != NO_CELL) flush(true, pkey, pcnt);
+        __syncwarp();
+        r = rn;
+        t = tn;
+        cs = ns;
+        buf ^= 1;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nloc; i += DEP_THREADS) {
-        const long long v = sacc[i];
+    if (dense) return;
+    for (int i = threadIdx.x; i < nloc; i += NW * 32) {
+        const long long v = (long long)shi[i] * (1ll << TILE_SPLIT) + (long long)slo[i];
         if (v != 0) {
             const int ly = i / SW, lx = i % SW;
             const int gx = wrap_i(x0 - 1 + lx, a.Nx), gy = wrap_i(y0 - 1 + ly, a.Ny);
@@ -785,7 +916,9 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs_tsc(DepArgs a) {
             }
         }
         const uint32_t kprev = __shfl_up_sync(FULL, ckey, 1);
-        const unsigned H = __ballot_sync(FULL, lane == 0 || ckey != kprev);
+        // a segment never spans lanes 15|16: a run total covers at most 64
+        // particles, |total| <= 64 * (2^24 + 3) < 2^31
+        const unsigned H = __ballot_sync(FULL, lane == 0 || lane == 16 || ckey != kprev);
         const int segstart = 31 - __clz(H & upto);
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -821,17 +954,31 @@ __global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double
     if (i < g) rho[i] = __dadd_rn(__dmul_rn((double)acc[i], unit), background);
 }
 
+template <int S, int LPP, int NW, int MINB>
+static void launch_tiled(pic_ctx* c, const DepArgs& a, unsigned tiles) {
+    const size_t smem =
+        tiled_stage_bytes<S, LPP, NW>() + (size_t)(a.tile_h + 3) * (a.tile_w + 3) * 2 * sizeof(uint32_t);
+    // dynamic shared memory above 48 KB must be opted into (once per kernel)
+    static size_t opted = 0;
+    if (smem > opted) {
+        cudaFuncSetAttribute(deposit_tiled<S, LPP, NW, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        opted = smem;
+    }
+    deposit_tiled<S, LPP, NW, MINB><<<tiles, NW * 32, smem, c->stream>>>(a);
+}
+
 template <int S>
 // kernel choice: 0 tiled (cell-sorted), 1 run-aggregating (any order), 2 one thread per particle
 static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
     if (kind == 0) {
-        const size_t smem = (size_t)(a.tile_h + 3) * (a.tile_w + 3) * sizeof(long long);
         const unsigned tiles = (unsigned)(a.tiles_x * ((c->Ny + a.tile_h - 1) / a.tile_h));
         prof_begin(c, "deposit");
+        // 8 particles per lane and stage, 4 warps per tile; TSC capped at 96
+        // registers (5 CTAs per SM), measured fastest at 1024^2 x 64 particles/cell
         if constexpr (S == S_TSC)
-            deposit_tiled_tsc<<<tiles, DEP_THREADS, smem, c->stream>>>(a);
+            launch_tiled<S, 8, 4, 5>(c, a, tiles);
         else
-            deposit_tiled<S><<<tiles, DEP_THREADS, smem, c->stream>>>(a);
+            launch_tiled<S, 8, 4, 4>(c, a, tiles);
         prof_end(c);
         return check_launch(c, "deposit_tiled");
     }

@@ -291,7 +291,8 @@ __global__ void __launch_bounds__(ENS_THREADS) ens_step_kernel(StepArgs a) {
                 }
             }
             const uint32_t kprev = __shfl_up_sync(FULLM, ckey, 1);
-            const unsigned H = __ballot_sync(FULLM, lane == 0 || ckey != kprev);
+            // segments stop at lane 16: a run total covers <= 64 particles and fits int32
+            const unsigned H = __ballot_sync(FULLM, lane == 0 || lane == 16 || ckey != kprev);
             const int segstart = 31 - __clz(H & upto);
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
@@ -386,7 +387,8 @@ __global__ void __launch_bounds__(ENS_THREADS) ens_deposit_tiled(StepArgs a, con
                 }
             }
             const uint32_t kprev = __shfl_up_sync(FULLM, ckey, 1);
-            const unsigned H = __ballot_sync(FULLM, lane == 0 || ckey != kprev);
+            // segments stop at lane 16: a run total covers <= 64 particles and fits int32
+            const unsigned H = __ballot_sync(FULLM, lane == 0 || lane == 16 || ckey != kprev);
             const int segstart = 31 - __clz(H & upto);
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {

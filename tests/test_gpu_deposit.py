@@ -177,6 +177,20 @@ def test_all_particles_in_one_cell(port, pg, scheme):
         check(port, pg, 16, 16, 16.0, 16.0, p, scheme, 0.5, order)
 
 
+@pytest.mark.parametrize("scheme", [NGP, CIC, TSC])
+@pytest.mark.parametrize("n", [131000, 200000])
+@pytest.mark.parametrize("order", ["sorted", "unsorted"])
+def test_dense_tile_same_sign(port, pg, scheme, n, order):
+    """Tiles below 2^17 particles use the split 32-bit shared accumulators,
+    denser ones add their runs straight to the global grid; both exact. Equal
+    charges at one corner node give the largest per-node sums (n * 2^24), and
+    long runs of them the largest int32 partial sums in a warp."""
+    rng = np.random.default_rng(n)
+    x = np.where(rng.random(n) < 0.5, 5.0, 5.0 + rng.random(n))
+    p = dict(x=x, y=np.full(n, 7.0), q=np.ones(n), vx=np.zeros(n), vy=np.zeros(n), m=np.ones(n))
+    check(port, pg, 16, 16, 16.0, 16.0, p, scheme, 0.0, order)
+
+
 @pytest.mark.parametrize("order", ["sorted", "unsorted"])
 def test_esirkepov_long_moves(port, pg, order):
     # moves of up to ~20 cells take the general trajectory loop
