@@ -61,7 +61,7 @@ extern "C" {
 
 /* ---- deposit ordering modes ---- */
 #define PIC_ORDER_AUTO 0     /* tiled kernel when cell-sorted, else the run-aggregating kernel   */
-#define PIC_ORDER_SORTED 1   /* tiled kernel; PIC_ERR_STATE unless cell-sorted                   */
+#define PIC_ORDER_SORTED 1   /* tiled kernel; PIC_ERR_STATE unless sorted (or only pushed since) */
 #define PIC_ORDER_UNSORTED 2 /* run-aggregating kernel (any order; fast when nearly sorted)      */
 #define PIC_ORDER_ATOMIC 3   /* one thread per particle, one int64 atomic per stencil node       */
 

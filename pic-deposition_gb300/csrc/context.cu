@@ -85,9 +85,6 @@ int check_device_status(pic_ctx* ctx) {
         case DEV_BAD_POSITION:
             return fail(PIC_ERR_DEVICE, "non-finite or out-of-range particle position (particle " +
                                             std::to_string(st.err_info) + ")");
-        case DEV_UNSORTED:
-            return fail(PIC_ERR_STATE, "sorted deposit met a particle outside its cell segment (index " +
-                                           std::to_string(st.err_info) + ")");
         case DEV_BAD_CELL:
             return fail(PIC_ERR_DEVICE, "cell key out of range (particle " + std::to_string(st.err_info) + ")");
         case DEV_MOVE_TOO_LARGE:
@@ -518,6 +515,7 @@ int pic_gpu_upload_particles(pic_ctx* c, const double* x, const double* y, const
     }
     c->n = n;
     c->sorted = 0;
+    c->part_valid = 0;
     if (n > 0) {
         normalize_charge<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->q, n, c->dstats);
         PIC_TRY(check_launch(c, "normalize_charge"));
@@ -535,6 +533,7 @@ int pic_gpu_upload_particles(pic_ctx* c, const double* x, const double* y, const
         PIC_TRY(build_offsets(c, c->cell));
         PIC_TRY(pic_gpu_synchronize(c));
         c->sorted = 1;
+        c->part_valid = 1;
     }
     return PIC_OK;
 }

@@ -593,6 +593,33 @@ __device__ __forceinline__ int tsc_true(int q, uint32_t acc, uint32_t cnt) {
     return tsc_central(q) ? (int)acc : (int)(acc - cnt * TSC_MAGIC_BITS);
 }
 
+// A particle outside the tile row whose slice of the stream holds it (the cell
+// ranges are those of an earlier sort and the particle has moved since): its
+// values go straight to the global int64 grid.
+template <int S>
+__device__ __forceinline__ void particle_to_global(const DepArgs& a, uint32_t key, float rx, float ry, float qn,
+                                                float vxx, float vyy, uint32_t p) {
+    constexpr int NV = Frame<S>::NX * Frame<S>::NX;
+    if (key >= (uint32_t)a.Nx * (uint32_t)a.Ny) {
+        set_dev_error(a.st, DEV_BAD_CELL, p);
+        return;
+    }
+    const int iy = (int)(key / (uint32_t)a.Nx), ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
+    int tv[NV];
+    if constexpr (S == S_TSC) {
+        uint32_t val[16];
+        tsc_values(rx, ry, qn, val);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) tv[q] = tsc_true(q, val[q], 1u);
+    } else {
+        int iv[Frame<S>::V];
+        if (!stencil_values<S>(a, rx, ry, qn, vxx, vyy, ix, iy, p, iv)) return;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) tv[q] = iv[q];
+    }
+    flush_global<S>(a, key, tv);
+}
+
 // Sorted path. One CTA of NW warps per tile of tile_w x tile_h cells. The
 // particles of one row of the tile are the contiguous slice
 // [offsets[c0], offsets[c0+tile_w]) of the cell-sorted stream; warp w walks
@@ -812,8 +839,13 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_tiled(DepArgs a) {
                 const uint32_t p = cstart + (uint32_t)(4 * h + k);
                 if (p - vbeg < vlen) {
                     const uint32_t key = u4(d.cell, k);
-                    if (key - c0 >= (uint32_t)tw) {
-                        set_dev_error(a.st, DEV_UNSORTED, p);
+                    if (key - c0 >= (uint32_t)tw) {  // left this tile row since the last sort
+                        float vxx = 0.0f, vyy = 0.0f;
+                        if constexpr (S == S_ESK) {
+                            vxx = f4(d.vx, k);
+                            vyy = f4(d.vy, k);
+                        }
+                        particle_to_global<S>(a, key, f4(d.xr, k), f4(d.yr, k), f4(d.q, k), vxx, vyy, p);
                         continue;
                     }
                     if (key != ckey) {  // a new run: divergent only at cell boundaries
@@ -1011,13 +1043,16 @@ int deposit_rho(pic_ctx* c, int scheme, double dt, double background) {
     if (scheme < PIC_SCHEME_NGP || scheme > PIC_SCHEME_ESIRKEPOV) return fail(PIC_ERR_ARG, "unknown scheme");
     int tiled;  // kernel kind, see launch_deposit
     if (c->order_mode == PIC_ORDER_SORTED) {
-        if (!c->sorted) return fail(PIC_ERR_STATE, "deposit: PIC_ORDER_SORTED needs cell-sorted particles");
+        if (!c->sorted && !c->part_valid)
+            return fail(PIC_ERR_STATE, "deposit: PIC_ORDER_SORTED needs cell-sorted particles");
         tiled = 0;
     } else if (c->order_mode == PIC_ORDER_UNSORTED) {
         tiled = 1;
     } else if (c->order_mode == PIC_ORDER_ATOMIC) {
         tiled = 2;
     } else {
+        // between sorts the run-aggregating kernel: particles of neighbouring
+        // cells interleave within a cell's range and break the lanes' runs
         tiled = c->sorted ? 0 : 1;
     }
     PIC_CUDA_TRY(cudaMemsetAsync(c->acc, 0, c->G * sizeof(long long), c->stream));

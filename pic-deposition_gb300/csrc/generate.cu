@@ -134,6 +134,7 @@ extern "C" int pic_gpu_generate(pic_ctx* c, const pic_gen_config* g) {
     c->n = g->n;
     c->has_mass = a.m ? 1 : 0;
     c->sorted = 0;
+    c->part_valid = 0;
     c->launches++;
     return pic_gpu_synchronize(c);
 }

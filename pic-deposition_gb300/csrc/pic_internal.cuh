@@ -28,7 +28,6 @@ struct DevStats {
 enum DevErr : int {
     DEV_OK = 0,
     DEV_BAD_POSITION = 1,   // non-finite or out-of-range position on upload
-    DEV_UNSORTED = 2,       // sorted kernel met a particle outside its row segment
     DEV_BAD_CELL = 3,       // cell key >= Nx*Ny
     DEV_MOVE_TOO_LARGE = 4, // trajectory longer than the general Esirkepov loop allows
     DEV_COURANT = 5,        // Esirkepov current with |v|*dt >= cell size
@@ -63,6 +62,10 @@ struct pic_ctx {
     float *xr = nullptr, *yr = nullptr, *vx = nullptr, *vy = nullptr, *q = nullptr, *m = nullptr;
     int has_mass = 0;
     int sorted = 0;  // particles are in stable cell order and `offsets` is valid
+    // `offsets` (from the last sort) still cut the particle array into the cells'
+    // ranges of that sort: kept by the push, which moves particles without
+    // reordering them; cleared when particles are replaced or reordered
+    int part_valid = 0;
 
     // sort scratch
     uint32_t *cell_alt = nullptr, *idx_a = nullptr, *idx_b = nullptr;

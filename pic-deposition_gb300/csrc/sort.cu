@@ -232,6 +232,7 @@ int sort_particles(pic_ctx* c) {
     const size_t n = c->n;
     if (n == 0) {
         c->sorted = 1;
+        c->part_valid = 1;
         return build_offsets(c, c->cell);
     }
     const unsigned tiles = (unsigned)((n + RS_TILE - 1) / RS_TILE);
@@ -292,6 +293,7 @@ int sort_particles(pic_ctx* c) {
     }
     PIC_TRY(build_offsets(c, c->cell));
     c->sorted = 1;
+    c->part_valid = 1;
     return PIC_OK;
 }
 

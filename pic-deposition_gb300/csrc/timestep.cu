@@ -80,7 +80,7 @@ struct Buffers {
     uint32_t *cell, *cell_alt, *idx_a, *idx_b;
     float *xr, *yr, *vx, *vy, *q, *m;
     float* alt[6];
-    int sorted;
+    int sorted, part_valid;
     bool operator==(const Buffers& o) const {
         return cell == o.cell && cell_alt == o.cell_alt && idx_a == o.idx_a && xr == o.xr && yr == o.yr &&
                vx == o.vx && vy == o.vy && q == o.q && m == o.m;
@@ -101,6 +101,7 @@ static Buffers buffers_of(const pic_ctx* c) {
     b.m = c->m;
     for (int k = 0; k < 6; ++k) b.alt[k] = c->alt[k];
     b.sorted = c->sorted;
+    b.part_valid = c->part_valid;
     return b;
 }
 
@@ -117,6 +118,7 @@ static void set_buffers(pic_ctx* c, const Buffers& b) {
     c->m = b.m;
     for (int k = 0; k < 6; ++k) c->alt[k] = b.alt[k];
     c->sorted = b.sorted;
+    c->part_valid = b.part_valid;
 }
 
 struct StepGraph {

@@ -145,6 +145,34 @@ def test_nearly_sorted_after_push(port, pg, scheme):
     assert unit == wunit and np.array_equal(acc, want) and np.array_equal(acc2, want)
 
 
+@pytest.mark.parametrize("scheme", [NGP, CIC, TSC, ESK])
+def test_pushed_since_sort_uses_stale_ranges(port, pg, scheme):
+    """After a sort and a push of several cells, PIC_ORDER_SORTED still walks the
+    sort's cell ranges; particles that left their tile row go straight to the
+    global grid. Bit-identical to the oracle and to the other kernels."""
+    p = maxwellian(port, 64, 48, 6.4, 4.8, 150000, seed=13, T=3.0)
+    with pg.Context(64, 48, 6.4, 4.8, len(p["x"])) as c:
+        c.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+        c.sort()
+        c.set_tile(16, 4)
+        c.push(0.2)
+        assert not c.is_sorted()
+        c.deposit(scheme, 0.02, download=False)
+        acc, unit = c.rho_fixed()
+        c.set_order(pg.ORDER_SORTED)
+        c.deposit(scheme, 0.02, download=False)
+        acc_s, _ = c.rho_fixed()
+        c.set_order(pg.ORDER_UNSORTED)
+        c.deposit(scheme, 0.02, download=False)
+        acc_u, _ = c.rho_fixed()
+        lay = c.device_layout()
+    _, maxq = port.normalize_charge(p["q"])
+    want, wunit = port.deposit_fixed(64, 48, 6.4, 4.8, scheme, lay["cell"], lay["xr"], lay["yr"], lay["q"], maxq,
+                                     lay["vx"], lay["vy"], 0.02)
+    assert unit == wunit
+    assert np.array_equal(acc, want) and np.array_equal(acc_s, want) and np.array_equal(acc_u, want)
+
+
 # ---- edge cases ------------------------------------------------------------
 @pytest.mark.parametrize("scheme", [NGP, CIC, TSC, ESK])
 @pytest.mark.parametrize("order", ["sorted", "unsorted"])
