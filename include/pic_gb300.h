@@ -159,7 +159,8 @@ int pic_gpu_sort(pic_ctx* ctx, uint32_t* keys_out, uint32_t* perm_out, uint32_t*
  *      dispatch (src/deposition/deposition.cpp:120-132,181-200) ---- */
 
 int pic_gpu_set_deposit_order(pic_ctx* ctx, int order);
-/* Tile of the sorted kernel, in cells (tile_w <= 64, tile_h <= 32). */
+/* Tile of the sorted kernel, in cells (tile_w <= 64, tile_h <= 32). Without
+ * this call the tile is chosen per deposit for about 8192 particles per tile. */
 int pic_gpu_set_tile(pic_ctx* ctx, int tile_w, int tile_h);
 /* Deposits rho for `scheme` (PIC_SCHEME_*) into the context's grid, adds
  * `background` to every node, and copies rho to `rho_out` (Nx*Ny doubles)

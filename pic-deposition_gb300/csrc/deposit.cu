@@ -1071,6 +1071,16 @@ int deposit_rho(pic_ctx* c, int scheme, double dt, double background) {
     a.dtf = (float)dt;
     a.dtdx = (float)(dt / c->dx);
     a.dtdy = (float)(dt / c->dy);
+    if (!c->tile_user) {
+        // about 8K particles per tile (measured best at 16 and 64 particles per
+        // cell), at least as many rows as the 4 warps of a CTA
+        const double ppc = (double)c->n / (double)c->G;
+        const double cells = ppc > 0.0 ? 8192.0 / ppc : 2048.0;
+        c->tile_w = cells <= 256.0 ? 32 : 64;
+        int h = 4;
+        while (h < 32 && (double)(c->tile_w * h * 2) <= cells) h *= 2;
+        c->tile_h = h;
+    }
     a.tile_w = c->tile_w;
     a.tile_h = c->tile_h;
     a.tiles_x = (c->Nx + c->tile_w - 1) / c->tile_w;
@@ -1120,6 +1130,7 @@ int pic_gpu_set_tile(pic_ctx* c, int tile_w, int tile_h) {
         return fail(PIC_ERR_ARG, "tile must be 1..64 x 1..32 cells");
     c->tile_w = tile_w;
     c->tile_h = tile_h;
+    c->tile_user = 1;
     return PIC_OK;
 }
 

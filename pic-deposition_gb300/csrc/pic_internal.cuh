@@ -121,6 +121,7 @@ struct pic_ctx {
     // tuning
     int order_mode = PIC_ORDER_AUTO;
     int tile_w = 32, tile_h = 8;
+    int tile_user = 0;  // tile shape set by pic_gpu_set_tile (else chosen per deposit)
 
     long long launches = 0;
 
