@@ -927,8 +927,6 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs_tsc(DepArgs a) {
                     set_dev_error(a.st, DEV_BAD_CELL, (unsigned)p);
                     continue;
                 }
-                uint32_t val[16];
-                tsc_values(f4(cur.xr, k), f4(cur.yr, k), f4(cur.q, k), val);
                 if (key != ckey) {
                     if (ckey != NO_CELL) {
                         int t[16];
@@ -937,14 +935,12 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs_tsc(DepArgs a) {
                         flush_global<S_TSC>(a, ckey, t);
                     }
                     ckey = key;
-                    cnt = 1;
+                    cnt = 0;
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) acc[q] = val[q];
-                } else {
-                    ++cnt;
-#pragma unroll
-                    for (int q = 0; q < 16; ++q) acc[q] += val[q];
+                    for (int q = 0; q < 16; ++q) acc[q] = 0;
                 }
+                tsc_accumulate(f4(cur.xr, k), f4(cur.yr, k), f4(cur.q, k), acc);
+                ++cnt;
             }
         }
         const uint32_t kprev = __shfl_up_sync(FULL, ckey, 1);
