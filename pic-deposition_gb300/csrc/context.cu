@@ -90,9 +90,6 @@ int check_device_status(pic_ctx* ctx) {
         case DEV_MOVE_TOO_LARGE:
             return fail(PIC_ERR_ARG, "trajectory longer than 256 cells in one step (particle " +
                                          std::to_string(st.err_info) + ")");
-        case DEV_TIMEOUT:
-            return fail(PIC_ERR_TIMEOUT, "a bounded device-side wait gave up (kernel step " +
-                                             std::to_string(st.err_info) + ")");
         case DEV_COURANT:
             return fail(PIC_ERR_COURANT, "Esirkepov current needs |v|*dt < cell size (particle " +
                                              std::to_string(st.err_info) + ")");

@@ -31,7 +31,6 @@ enum DevErr : int {
     DEV_BAD_CELL = 3,       // cell key >= Nx*Ny
     DEV_MOVE_TOO_LARGE = 4, // trajectory longer than the general Esirkepov loop allows
     DEV_COURANT = 5,        // Esirkepov current with |v|*dt >= cell size
-    DEV_TIMEOUT = 6,        // a bounded wait on a copy or barrier gave up
 };
 
 // Particle arrays are allocated this many elements longer than the capacity:
