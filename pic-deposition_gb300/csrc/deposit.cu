@@ -367,6 +367,26 @@ __device__ __forceinline__ void flush_global(const DepArgs& a, uint32_t key, con
     }
 }
 
+// flush_global without integer division (the any-order kernels flush once per
+// run of a warp step; measured faster there, while the tiled kernel keeps the
+// plain form above).
+template <int S>
+__device__ __forceinline__ void flush_global_nd(const DepArgs& a, uint32_t key, float inv_nx,
+                                                const int (&acc)[Frame<S>::NX * Frame<S>::NX]) {
+    constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO;
+    int iy, ix;
+    split_key(key, a.Nx, inv_nx, iy, ix);
+#pragma unroll
+    for (int j = 0; j < NX; ++j) {
+        const size_t row = (size_t)wrap_near(iy + LO + j, a.Ny) * a.Nx;
+#pragma unroll
+        for (int i = 0; i < NX; ++i) {
+            const int v = acc[j * NX + i];
+            if (v != 0) atomicAdd(a.acc + row + wrap_near(ix + LO + i, a.Nx), (unsigned long long)(long long)v);
+        }
+    }
+}
+
 // Any-order path with run aggregation: the sorted path's warp step (4
 // consecutive particles per lane, register sums per cell, segmented warp scan)
 // over the whole particle array, with the run totals added straight to the
@@ -381,6 +401,7 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs(DepArgs a) {
     const size_t gw = (size_t)blockIdx.x * DEP_WARPS + (threadIdx.x >> 5);
     const size_t stride = (size_t)gridDim.x * DEP_WARPS * 128;
     const uint32_t G = (uint32_t)a.Nx * (uint32_t)a.Ny;
+    const float inv_nx = 1.0f / (float)a.Nx;
     const unsigned upto = (lane == 31) ? FULL : ((2u << lane) - 1u);
     size_t base = gw * 128;
     Quad<S> cur, nxt;
@@ -401,7 +422,8 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs(DepArgs a) {
                     set_dev_error(a.st, DEV_BAD_CELL, (unsigned)p);
                     continue;
                 }
-                const int iy = (int)(key / (uint32_t)a.Nx);
+                int iy, ixk;
+                split_key(key, a.Nx, inv_nx, iy, ixk);
                 int val[V];
                 float vxx = 0.0f, vyy = 0.0f;
                 if constexpr (S == S_ESK) {
@@ -409,10 +431,10 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs(DepArgs a) {
                     vyy = f4(cur.vy, k);
                 }
                 if (!stencil_values<S>(a, f4(cur.xr, k), f4(cur.yr, k), f4(cur.q, k), vxx, vyy,
-                                       (int)(key - (uint32_t)iy * (uint32_t)a.Nx), iy, p, val))
+                                       ixk, iy, p, val))
                     continue;
                 if (key != ckey) {
-                    if (ckey != NO_CELL) flush_global<S>(a, ckey, acc);
+                    if (ckey != NO_CELL) flush_global_nd<S>(a, ckey, inv_nx, acc);
                     ckey = key;
 #pragma unroll
                     for (int q = 0; q < NV; ++q) acc[q] = val[q];
@@ -437,7 +459,7 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs(DepArgs a) {
             }
         }
         const bool tail = (lane == 31) || ((H >> (lane + 1)) & 1u);
-        if (tail && ckey != NO_CELL) flush_global<S>(a, ckey, acc);
+        if (tail && ckey != NO_CELL) flush_global_nd<S>(a, ckey, inv_nx, acc);
         cur = nxt;
     }
 }
@@ -915,6 +937,7 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs_tsc(DepArgs a) {
     const size_t gw = (size_t)blockIdx.x * DEP_WARPS + (threadIdx.x >> 5);
     const size_t stride = (size_t)gridDim.x * DEP_WARPS * 128;
     const uint32_t G = (uint32_t)a.Nx * (uint32_t)a.Ny;
+    const float inv_nx = 1.0f / (float)a.Nx;
     const unsigned upto = (lane == 31) ? FULL : ((2u << lane) - 1u);
     size_t base = gw * 128;
     Quad<S_TSC> cur, nxt;
@@ -940,7 +963,7 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs_tsc(DepArgs a) {
                         int t[16];
 #pragma unroll
                         for (int q = 0; q < 16; ++q) t[q] = tsc_true(q, acc[q], cnt);
-                        flush_global<S_TSC>(a, ckey, t);
+                        flush_global_nd<S_TSC>(a, ckey, inv_nx, t);
                     }
                     ckey = key;
                     cnt = 0;
@@ -972,7 +995,7 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs_tsc(DepArgs a) {
             int t[16];
 #pragma unroll
             for (int q = 0; q < 16; ++q) t[q] = tsc_true(q, acc[q], cnt);
-            flush_global<S_TSC>(a, ckey, t);
+            flush_global_nd<S_TSC>(a, ckey, inv_nx, t);
         }
         cur = nxt;
     }

@@ -212,6 +212,38 @@ __device__ __forceinline__ int wrap_i(int i, int n) {
     return r < 0 ? r + n : r;
 }
 
+// i mod n without a division when i lies within one period of [0, n) (a
+// neighbour node or a move of at most one grid length); wrap_i otherwise.
+__device__ __forceinline__ int wrap_near(int i, int n) {
+    if (i >= n)
+        i -= n;
+    else if (i < 0)
+        i += n;
+    return (unsigned)i < (unsigned)n ? i : wrap_i(i, n);
+}
+
+// key = iy * n + ix split without an integer division: for key < 2^24 the FP32
+// quotient key * (1/n) is within one of floor(key / n), and one correction
+// step makes it exact; larger keys divide.
+__device__ __forceinline__ void split_key(uint32_t key, int n, float inv_n, int& iy, int& ix) {
+    if (key < (1u << 24)) {
+        int q = (int)((float)key * inv_n);
+        int r = (int)key - q * n;
+        if (r < 0) {
+            --q;
+            r += n;
+        } else if (r >= n) {
+            ++q;
+            r -= n;
+        }
+        iy = q;
+        ix = r;
+    } else {
+        iy = (int)(key / (uint32_t)n);
+        ix = (int)(key - (uint32_t)iy * (uint32_t)n);
+    }
+}
+
 __device__ __forceinline__ void set_dev_error(DevStats* st, int code, unsigned int info) {
     if (atomicCAS(&st->err, 0, code) == 0) st->err_info = info;
 }

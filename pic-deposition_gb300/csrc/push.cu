@@ -45,20 +45,21 @@ __device__ __forceinline__ void drift(float& r, int& i, float v, float dtd, int 
     const float x = r + v * dtd;
     const float s = floorf(x);
     r = x - s;
-    i = wrap_i(i + (int)s, n);
+    i = wrap_near(i + (int)s, n);
 }
 
 template <bool GATHER, bool PUSH>
 __global__ void __launch_bounds__(256) move_particles(MoveArgs a) {
     const float maxq = load_maxq(a.st);
+    const float inv_nx = 1.0f / (float)a.Nx;
     for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += (size_t)gridDim.x * blockDim.x) {
         const uint32_t key = a.cell[p];
-        int iy = (int)(key / (uint32_t)a.Nx);
-        int ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
+        int iy, ix;
+        split_key(key, a.Nx, inv_nx, iy, ix);
         float rx = a.xr[p], ry = a.yr[p];
         float vxx = a.vx[p], vyy = a.vy[p];
         if constexpr (GATHER) {
-            const int ixp = (ix + 1) % a.Nx, iyp = (iy + 1) % a.Ny;
+            const int ixp = ix + 1 == a.Nx ? 0 : ix + 1, iyp = iy + 1 == a.Ny ? 0 : iy + 1;
             const size_t i00 = (size_t)iy * a.Nx + ix, i10 = (size_t)iy * a.Nx + ixp;
             const size_t i01 = (size_t)iyp * a.Nx + ix, i11 = (size_t)iyp * a.Nx + ixp;
             const float ex = interp(a.Exf, i00, i10, i01, i11, rx, ry);
