@@ -516,6 +516,7 @@ int pic_gpu_upload_particles(pic_ctx* c, const double* x, const double* y, const
     c->n = n;
     c->sorted = 0;
     c->part_valid = 0;
+    c->qsum_valid = 0;
     if (n > 0) {
         normalize_charge<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->q, n, c->dstats);
         PIC_TRY(check_launch(c, "normalize_charge"));

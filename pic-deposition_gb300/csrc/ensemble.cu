@@ -980,6 +980,7 @@ int pic_ens_create(const pic_ens_member* runs_in, int nruns, const pic_ens_confi
         c->has_mass = 0;
         c->sorted = 0;
         c->part_valid = 0;
+        c->qsum_valid = 0;
     }
     // batched FFT plans per grid size
     size_t spec_total = 0;

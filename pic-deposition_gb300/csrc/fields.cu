@@ -46,6 +46,7 @@ enum SumKind : int {
     SUM_Q = 2,         // sum qn[i]*maxq
     SUM_ABS_Q = 3,     // sum |qn[i]*maxq|
     SUM_KE = 4,        // sum 0.5*m*(vx^2+vy^2)
+    SUM_V2 = 5,        // sum vx^2+vy^2 (unit masses; halved once at the end)
 };
 
 struct SumArgs {
@@ -70,6 +71,10 @@ __device__ __forceinline__ double sum_item(const SumArgs& a, size_t i) {
             return (double)(a.q[i] * load_maxq(a.st));
         case SUM_ABS_Q:
             return fabs((double)(a.q[i] * load_maxq(a.st)));
+        case SUM_V2: {
+            const double vx = a.vx[i], vy = a.vy[i];
+            return __dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy));
+        }
         default: {
             const double vx = a.vx[i], vy = a.vy[i];
             const double m = a.m ? (double)a.m[i] : 1.0;
@@ -88,19 +93,26 @@ __global__ void __launch_bounds__(RED_THREADS) sum_partials(SumArgs a, double* _
     if (threadIdx.x == 0) partial[blockIdx.x] = t;
 }
 
-__global__ void __launch_bounds__(RED_THREADS) sum_final(const double* __restrict__ partial, double* out) {
+__global__ void __launch_bounds__(RED_THREADS) sum_final(const double* __restrict__ partial, double scale,
+                                                        double* out) {
     double s = 0.0;
     for (int i = threadIdx.x; i < RED_BLOCKS; i += RED_THREADS) s = __dadd_rn(s, partial[i]);
     const double t = block_sum(s);
-    if (threadIdx.x == 0) *out = t;
+    if (threadIdx.x == 0) *out = __dmul_rn(t, scale);
 }
 
-// Queues one deterministic sum into slot `out` (device).
-int device_sum(pic_ctx* c, const SumArgs& a, double* out) {
+// Queues one deterministic sum into slot `out` (device), times `scale`.
+int device_sum(pic_ctx* c, const SumArgs& a, double* out, double scale) {
     sum_partials<<<RED_BLOCKS, RED_THREADS, 0, c->stream>>>(a, c->red_partials);
     PIC_TRY(check_launch(c, "sum_partials"));
-    sum_final<<<1, RED_THREADS, 0, c->stream>>>(c->red_partials, out);
+    sum_final<<<1, RED_THREADS, 0, c->stream>>>(c->red_partials, scale, out);
     return check_launch(c, "sum_final");
+}
+int device_sum(pic_ctx* c, const SumArgs& a, double* out) { return device_sum(c, a, out, 1.0); }
+
+__global__ void copy_charge_sums(double* r) {
+    r[1] = r[8];
+    r[6] = r[9];
 }
 
 // ---- Poisson ---------------------------------------------------------------
@@ -314,12 +326,19 @@ int diagnostics_async(pic_ctx* c) {
     a.vy = c->vy;
     a.m = c->has_mass ? c->m : nullptr;
     a.n = c->n;
-    a.kind = SUM_Q;
-    PIC_TRY(device_sum(c, a, c->red_out + 1));  // total_charge
-    a.kind = SUM_ABS_Q;
-    PIC_TRY(device_sum(c, a, c->red_out + 6));  // sum |q|
-    a.kind = SUM_KE;
-    PIC_TRY(device_sum(c, a, c->red_out + 3));  // kinetic
+    if (!c->qsum_valid) {  // total charge and sum |q| change only with the particle set
+        a.kind = SUM_Q;
+        PIC_TRY(device_sum(c, a, c->red_out + 8));
+        a.kind = SUM_ABS_Q;
+        PIC_TRY(device_sum(c, a, c->red_out + 9));
+        c->qsum_valid = 1;
+    }
+    copy_charge_sums<<<1, 1, 0, c->stream>>>(c->red_out);  // total_charge, sum |q|
+    PIC_TRY(check_launch(c, "copy_charge_sums"));
+    // kinetic: sum 0.5*m*v^2; with unit masses the 0.5 is applied once to the sum
+    // (halving commutes with every rounded addition: the same bits)
+    a.kind = a.m ? SUM_KE : SUM_V2;
+    PIC_TRY(device_sum(c, a, c->red_out + 3, a.m ? 1.0 : 0.5));
     SumArgs g{};
     g.n = c->G;
     g.kind = SUM_GRID;

@@ -135,6 +135,7 @@ extern "C" int pic_gpu_generate(pic_ctx* c, const pic_gen_config* g) {
     c->has_mass = a.m ? 1 : 0;
     c->sorted = 0;
     c->part_valid = 0;
+    c->qsum_valid = 0;
     c->launches++;
     return pic_gpu_synchronize(c);
 }

@@ -99,6 +99,9 @@ struct pic_ctx {
     // deterministic FP64 reductions
     double* red_partials = nullptr;
     double* red_out = nullptr;
+    // red_out[8], red_out[9] hold sum(q) and sum(|q|) of the current particle set:
+    // charges do not change while particles move or are sorted
+    int qsum_valid = 0;
     // red-black Gauss-Seidel
     double *rb_b = nullptr, *rb_partial = nullptr, *rb_scalars = nullptr;
     double* rb_ps = nullptr;   // persistent solve: partial sums, barrier, results
