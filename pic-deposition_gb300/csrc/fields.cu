@@ -46,7 +46,6 @@ enum SumKind : int {
     SUM_Q = 2,         // sum qn[i]*maxq
     SUM_ABS_Q = 3,     // sum |qn[i]*maxq|
     SUM_KE = 4,        // sum 0.5*m*(vx^2+vy^2)
-    SUM_V2 = 5,        // sum vx^2+vy^2 (unit masses; halved once at the end)
 };
 
 struct SumArgs {
@@ -71,10 +70,6 @@ __device__ __forceinline__ double sum_item(const SumArgs& a, size_t i) {
             return (double)(a.q[i] * load_maxq(a.st));
         case SUM_ABS_Q:
             return fabs((double)(a.q[i] * load_maxq(a.st)));
-        case SUM_V2: {
-            const double vx = a.vx[i], vy = a.vy[i];
-            return __dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy));
-        }
         default: {
             const double vx = a.vx[i], vy = a.vy[i];
             const double m = a.m ? (double)a.m[i] : 1.0;
@@ -90,6 +85,39 @@ __global__ void __launch_bounds__(RED_THREADS) sum_partials(SumArgs a, double* _
     double s = 0.0;
     for (size_t i = b + threadIdx.x; i < e; i += RED_THREADS) s = __dadd_rn(s, sum_item(a, i));
     const double t = block_sum(s);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+// Sum of vx^2 + vy^2 over the particles with no FP64 arithmetic per particle
+// (FP64 is slow on this part): each square is formed exactly as an FP32 pair
+// (product and its fused-multiply-add error), each thread accumulates in
+// double-FP32 (Knuth's two-sum keeps the running sum's rounding errors), and the
+// threads' totals enter the same deterministic FP64 block and grid sums. Agrees
+// with an FP64 sum of the squares to about 1e-14 relative.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float t) {
+    const float s = __fadd_rn(hi, t);
+    const float v = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, v)), __fsub_rn(t, v));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+
+__global__ void __launch_bounds__(RED_THREADS) sum_v2_partials(const float* __restrict__ vx,
+                                                              const float* __restrict__ vy, size_t n,
+                                                              double* __restrict__ partial) {
+    const size_t chunk = (n + RED_BLOCKS - 1) / RED_BLOCKS;
+    const size_t b = (size_t)blockIdx.x * chunk;
+    const size_t e = b + chunk < n ? b + chunk : n;
+    float hi = 0.0f, lo = 0.0f;
+    for (size_t i = b + threadIdx.x; i < e; i += RED_THREADS) {
+        const float x = vx[i], y = vy[i];
+        const float px = __fmul_rn(x, x), py = __fmul_rn(y, y);
+        const float ex = __fmaf_rn(x, x, -px), ey = __fmaf_rn(y, y, -py);
+        two_sum_acc(hi, lo, px);
+        two_sum_acc(hi, lo, py);
+        lo = __fadd_rn(lo, __fadd_rn(ex, ey));
+    }
+    const double t = block_sum(__dadd_rn((double)hi, (double)lo));
     if (threadIdx.x == 0) partial[blockIdx.x] = t;
 }
 
@@ -335,10 +363,19 @@ int diagnostics_async(pic_ctx* c) {
     }
     copy_charge_sums<<<1, 1, 0, c->stream>>>(c->red_out);  // total_charge, sum |q|
     PIC_TRY(check_launch(c, "copy_charge_sums"));
-    // kinetic: sum 0.5*m*v^2; with unit masses the 0.5 is applied once to the sum
-    // (halving commutes with every rounded addition: the same bits)
-    a.kind = a.m ? SUM_KE : SUM_V2;
-    PIC_TRY(device_sum(c, a, c->red_out + 3, a.m ? 1.0 : 0.5));
+    // kinetic: sum 0.5*m*v^2 in FP64 per particle when masses differ from 1;
+    // with unit masses 0.5 * sum v^2 (double-FP32 per thread, FP64 across threads)
+    if (a.m) {
+        a.kind = SUM_KE;
+        PIC_TRY(device_sum(c, a, c->red_out + 3));
+    } else if (c->n > 0) {
+        sum_v2_partials<<<RED_BLOCKS, RED_THREADS, 0, c->stream>>>(c->vx, c->vy, c->n, c->red_partials);
+        PIC_TRY(check_launch(c, "sum_v2_partials"));
+        sum_final<<<1, RED_THREADS, 0, c->stream>>>(c->red_partials, 0.5, c->red_out + 3);
+        PIC_TRY(check_launch(c, "sum_final"));
+    } else {
+        PIC_CUDA_TRY(cudaMemsetAsync(c->red_out + 3, 0, sizeof(double), c->stream));
+    }
     SumArgs g{};
     g.n = c->G;
     g.kind = SUM_GRID;
