@@ -5,6 +5,9 @@
 // Per step, for NGP/CIC/TSC (simulation.cpp:94-98, 101-105, 120-131):
 //     push(dt) -> [cell sort, every sort_interval steps] -> deposit -> + background
 //     -> Poisson -> gather(dt) -> diagnostics
+// where a step's gather runs in one pass with the next step's push (same
+// arithmetic, one read and write of the particles fewer) and its diagnostics
+// right after that pass.
 // and for the trajectory-averaged ("Esirkepov") rho:
 //     deposit(dt) -> + background -> Poisson -> push(dt) -> gather(dt) -> diagnostics.
 // The reference sorts a copy of the particles inside every deposit
@@ -56,18 +59,37 @@ static int solve(pic_ctx* c, const pic_run_config* cfg) {
     return cfg->rbgs_warm > 0 ? ws_record_solution(c) : PIC_OK;
 }
 
-// One step; `do_sort` selects the variant with the cell sort.
-static int one_step(pic_ctx* c, const pic_run_config* cfg, bool do_sort, double* hist, int* step_ctr, int steps) {
-    const bool esk = cfg->scheme == PIC_SCHEME_ESIRKEPOV;
-    if (!esk) PIC_TRY(move(c, cfg->dt, false, true));
-    if (do_sort) PIC_TRY(sort_particles(c));
-    PIC_TRY(deposit_rho(c, cfg->scheme, cfg->dt, cfg->background));
-    PIC_TRY(solve(c, cfg));
-    if (esk) PIC_TRY(move(c, cfg->dt, false, true));
-    PIC_TRY(move(c, cfg->dt, true, false));
+// The diagnostics of the step whose gather has just run.
+static int record_step(pic_ctx* c, double* hist, int* step_ctr, int steps) {
     PIC_TRY(diagnostics_async(c));
     finalize_diag<<<1, 1, 0, c->stream>>>(c->red_out, c->dx * c->dy, hist, step_ctr, steps);
     return check_launch(c, "finalize_diag");
+}
+
+// One step; `do_sort` selects the variant with the cell sort. For NGP/CIC/TSC
+// the step ends after its Poisson solve with its gather pending: with `head`,
+// the previous step's gather runs fused with this step's push (kick of step
+// s-1 and drift of step s in one pass over the particles, push.cu's fused
+// kernel), then the previous step's diagnostics (the push leaves the velocities
+// unchanged); the last step's gather runs after the loop.
+static int one_step(pic_ctx* c, const pic_run_config* cfg, bool do_sort, double* hist, int* step_ctr, int steps,
+                    bool head) {
+    if (cfg->scheme == PIC_SCHEME_ESIRKEPOV) {
+        PIC_TRY(deposit_rho(c, cfg->scheme, cfg->dt, cfg->background));
+        PIC_TRY(solve(c, cfg));
+        PIC_TRY(move(c, cfg->dt, false, true));
+        PIC_TRY(move(c, cfg->dt, true, false));
+        return record_step(c, hist, step_ctr, steps);
+    }
+    if (head) {
+        PIC_TRY(move(c, cfg->dt, true, true));
+        PIC_TRY(record_step(c, hist, step_ctr, steps));
+    } else {
+        PIC_TRY(move(c, cfg->dt, false, true));
+    }
+    if (do_sort) PIC_TRY(sort_particles(c));
+    PIC_TRY(deposit_rho(c, cfg->scheme, cfg->dt, cfg->background));
+    return solve(c, cfg);
 }
 
 // The cell sort ping-pongs the particle arrays with their scratch copies by
@@ -129,13 +151,13 @@ struct StepGraph {
 };
 
 static int capture(pic_ctx* c, const pic_run_config* cfg, bool do_sort, double* hist, int* ctr, int steps,
-                   cudaGraphExec_t* out) {
+                   bool head, cudaGraphExec_t* out) {
     const int prof = c->prof_enabled;
     c->prof_enabled = 0;
     cudaGraph_t g = nullptr;
     const long long l0 = c->launches;
     PIC_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    const int rc = one_step(c, cfg, do_sort, hist, ctr, steps);
+    const int rc = one_step(c, cfg, do_sort, hist, ctr, steps, head);
     const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->prof_enabled = prof;
     (do_sort ? c->graph_launches_sort : c->graph_launches_plain) = c->launches - l0;
@@ -181,10 +203,12 @@ int run_steps(pic_ctx* c, const pic_run_config* cfg, int steps, pic_diag* histor
         const int k = cfg->sort_interval;
         // the Gauss-Seidel stop is decided on the host, so those steps run eagerly
         const bool graph = cfg->use_graph && cfg->poisson == 0;
+        const bool esk = cfg->scheme == PIC_SCHEME_ESIRKEPOV;
         for (int s = 0; s < steps; ++s) {
             const bool do_sort = k > 0 && (s % k) == 0;
+            const bool head = s > 0;  // the previous step's gather is pending (NGP/CIC/TSC)
             if (!graph || s == 0) {
-                PIC_TRY(one_step(c, cfg, do_sort, hist, ctr, steps));
+                PIC_TRY(one_step(c, cfg, do_sort, hist, ctr, steps, head));
                 continue;
             }
             const Buffers now = buffers_of(c);
@@ -195,7 +219,7 @@ int run_steps(pic_ctx* c, const pic_run_config* cfg, int steps, pic_diag* histor
                 StepGraph sg;
                 sg.do_sort = do_sort;
                 sg.before = now;
-                PIC_TRY(capture(c, cfg, do_sort, hist, ctr, steps, &sg.exec));
+                PIC_TRY(capture(c, cfg, do_sort, hist, ctr, steps, head, &sg.exec));
                 sg.after = buffers_of(c);  // the capture ran the host side: pointers as the graph leaves them
                 sg.kernels = do_sort ? c->graph_launches_sort : c->graph_launches_plain;
                 graphs.push_back(sg);
@@ -204,6 +228,10 @@ int run_steps(pic_ctx* c, const pic_run_config* cfg, int steps, pic_diag* histor
             PIC_CUDA_TRY(cudaGraphLaunch(g->exec, c->stream));
             set_buffers(c, g->after);
             c->launches += g->kernels;
+        }
+        if (!esk) {  // the last step's gather and diagnostics
+            PIC_TRY(move(c, cfg->dt, true, false));
+            PIC_TRY(record_step(c, hist, ctr, steps));
         }
         if (history)
             PIC_CUDA_TRY(cudaMemcpyAsync(history, hist, (size_t)steps * 6 * sizeof(double), cudaMemcpyDeviceToHost,
