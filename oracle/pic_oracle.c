@@ -608,9 +608,10 @@ double orc_charge_error(double integrated_rho, double total_charge, double abs_c
 /* so |qn| <= 1 and a uniform |q| gives qn = +-1 exactly. a = qn * 2^24 and  */
 /* A = rint(a) is the particle's charge in units. Every frame node gets      */
 /* v = rint((a * Y[j]) * X[i]) (FP32 products, round to nearest even), then   */
-/* the node of largest weight (first maximum of X and of Y) gets              */
-/* A - (sum of the others), so a particle deposits exactly A units and the    */
-/* grid's total charge is exact. Sums are int64.                             */
+/* one node gets A - (sum of the others), so a particle deposits exactly A    */
+/* units and the grid's total charge is exact: for TSC the node of the        */
+/* particle's own cell (frame offset 0, weight >= 1/64), otherwise the node   */
+/* of largest weight (first maximum of X and of Y). Sums are int64.           */
 /* unit = ((double)maxq * inv_vol) * 2^-24; rho = acc * unit + background.   */
 /* ======================================================================= */
 void orc_to_device(const orc_domain* d, size_t n, const double* x, const double* y, uint32_t* cell, float* xr,
@@ -826,7 +827,9 @@ int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t*
         } else {
             return -1;
         }
-        const int mx = first_max(X, nxf), my = first_max(Y, nyf);
+        /* TSC: the particle's own cell node (frame offset 0) */
+        const int mx = scheme == ORC_TSC ? -xlo : first_max(X, nxf);
+        const int my = scheme == ORC_TSC ? -ylo : first_max(Y, nyf);
         int64_t others = 0;
         for (int j = 0; j < nyf; ++j) {
             const float ay = a * Y[j];

@@ -7,8 +7,9 @@
 //
 //  * Fixed point. The resident charge is qn = q/max|q|; a particle carries
 //    A = rint(qn*2^24) units. Each stencil value (qn*2^24*Y[j])*X[i] (FP32) is
-//    rounded to the nearest int32, and the node of largest weight takes
-//    A - (sum of the others), so every particle deposits exactly A units and
+//    rounded to the nearest int32, and one node takes A - (sum of the others)
+//    (TSC: the particle's own cell node, weight >= 1/64; NGP/CIC/ESK: the node
+//    of largest weight), so every particle deposits exactly A units and
 //    total charge is exact. Sums are int64, so the result does not depend on
 //    summation order: the tiled, atomic and oracle paths agree bit for bit.
 //  * Sorted path (deposit_tiled). One CTA per tile of tile_w x tile_h cells;
@@ -301,7 +302,8 @@ __device__ __forceinline__ bool stencil_values(const DepArgs& a, float rx, float
             sum += val[j * NX + i];
         }
     }
-    const int kmaj = first_max(Y) * NX + first_max(X);
+    // TSC: the particle's own cell node (frame entry (1,1)); else the first largest weight
+    const int kmaj = S == S_TSC ? NX + 1 : first_max(Y) * NX + first_max(X);
     const int rem = A - sum;
 #pragma unroll
     for (int k = 0; k < NX * NX; ++k) val[k] += (k == kmaj) ? rem : 0;
@@ -497,8 +499,7 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_atomic(DepArgs a) {
 //    or t = r - 1 (r >= 0.5), the three non-zero weights are 0.5*(0.5-t)^2,
 //    0.75-t^2, 0.5*(0.5+t)^2 at frame columns 0..2 or 1..3 (each operation gives
 //    the bits the branchy form gives: r - 1, 0.5 - t and 0.5 + t are exact there);
-//  * the node of largest weight is always in rows and columns 1..2 of the frame,
-//    so the remainder goes to one of 4 entries;
+//  * the remainder goes to frame entry (1,1), the particle's own cell node;
 //  * the 12 entries outside rows and columns 1..2 involve an outer weight <= 1/8,
 //    so |value| < 2^22 and rint is one FP32 add of 1.5*2^23 (round to nearest
 //    even on the integer grid): the accumulators keep those entries with the
@@ -564,7 +565,6 @@ __device__ __forceinline__ void tsc_accumulate(float rx, float ry, float qn, uin
     f2_unpack(R2, Rx, Ry);
     const float X0 = sx ? 0.0f : Lx, X1 = sx ? Lx : Cx, X2 = sx ? Cx : Rx, X3 = sx ? Rx : 0.0f;
     const float Y0 = sy ? 0.0f : Ly, Y1 = sy ? Ly : Cy, Y2 = sy ? Cy : Ry, Y3 = sy ? Ry : 0.0f;
-    const int kx = X2 > X1 ? 2 : 1, ky = Y2 > Y1 ? 2 : 1;
     const f32x2 aq2 = f2_pack(aq, aq);
     float ay[4];
     f2_unpack(f2_mul(aq2, f2_pack(Y0, Y1)), ay[0], ay[1]);
@@ -596,11 +596,7 @@ __device__ __forceinline__ void tsc_accumulate(float rx, float ry, float qn, uin
         acc[j * 4 + 3] += e3;
         sum += e0 + e1 + e2 + e3;
     }
-    const uint32_t rem = (uint32_t)A - (sum - 12u * TSC_MAGIC_BITS);
-    acc[5] += (ky == 1 && kx == 1) ? rem : 0u;
-    acc[6] += (ky == 1 && kx == 2) ? rem : 0u;
-    acc[9] += (ky == 2 && kx == 1) ? rem : 0u;
-    acc[10] += (ky == 2 && kx == 2) ? rem : 0u;
+    acc[5] += (uint32_t)A - (sum - 12u * TSC_MAGIC_BITS);  // the remainder: own cell node
 }
 
 // One particle's frame values (tsc_accumulate into zeros).

@@ -12,8 +12,8 @@
 // array (8 MiB) until the process exits.
 //
 // The arithmetic is the one of the unsorted (global-atomic) deposit: the same
-// FP32 stencil frames, the same rounding to int32 units with the largest-weight
-// node taking each particle's remainder, and the same FP64 conversion, so the
+// FP32 stencil frames, the same rounding to int32 units with the same node taking
+// each particle's remainder, and the same FP64 conversion, so the
 // result equals pic_gpu_deposit's bit for bit on the same particles.
 #include <mutex>
 
@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(THREADS) deposit_kernel(Args a) {
                 sum += val[j * NX + i];
             }
         }
-        const int kmaj = first_max(Y) * NX + first_max(X);
+        // TSC: the particle's own cell node (frame entry (1,1)); else the first largest weight
+        const int kmaj = S == PIC_SCHEME_TSC ? NX + 1 : first_max(Y) * NX + first_max(X);
 #pragma unroll
         for (int j = 0; j < NX; ++j) {
             const size_t row = (size_t)wrap_i(iy + LO + j, a.Ny) * a.Nx;
