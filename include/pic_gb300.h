@@ -146,6 +146,9 @@ int pic_gpu_num_particles(pic_ctx* ctx, size_t* n_out);
 /* 1 when the resident particles are in cell order with valid per-cell offsets
  * (after pic_gpu_sort, or after an upload whose keys were already non-decreasing). */
 int pic_gpu_is_sorted(pic_ctx* ctx, int* sorted_out);
+/* The stored charge q/max|q| shared by every resident particle (+-1), or 0 when
+ * the charges differ. With one charge the kernels do not read the charge stream. */
+int pic_gpu_charge_uniform(pic_ctx* ctx, float* qn_out);
 
 /* ---- cell sort: replaces pic::sortParticlesByCell(ParticlesSoA&, const Domain&)
  *      (src/sorting/cell_sort.hpp:8-11, cell_sort.cpp:22-46) ---- */

@@ -275,6 +275,15 @@ __global__ void normalize_charge(float* __restrict__ q, size_t n, const DevStats
     if (i < n) q[i] = mq > 0.0f ? __fdiv_rn(q[i], mq) : 0.0f;
 }
 
+// Flags stored charges that differ from the first particle's (bitwise).
+__global__ void check_uniform_charge(const float* __restrict__ q, size_t n, DevStats* st) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const float q0 = q[0];
+    if (i == 0) st->q_first = q0;
+    const bool diff = i < n && __float_as_uint(q[i]) != __float_as_uint(q0);
+    if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(&st->q_mixed, 1u);
+}
+
 // Counts adjacent pairs out of cell order (0 => the upload is already sorted).
 __global__ void count_order_breaks(const uint32_t* __restrict__ cell, size_t n, DevStats* st) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -517,9 +526,12 @@ int pic_gpu_upload_particles(pic_ctx* c, const double* x, const double* y, const
     c->sorted = 0;
     c->part_valid = 0;
     c->qsum_valid = 0;
+    c->qn_uniform = 0.0f;
     if (n > 0) {
         normalize_charge<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->q, n, c->dstats);
         PIC_TRY(check_launch(c, "normalize_charge"));
+        check_uniform_charge<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->q, n, c->dstats);
+        PIC_TRY(check_launch(c, "check_uniform_charge"));
     }
     if (n > 1) {
         count_order_breaks<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->cell, n, c->dstats);
@@ -528,6 +540,7 @@ int pic_gpu_upload_particles(pic_ctx* c, const double* x, const double* y, const
     PIC_TRY(pic_gpu_synchronize(c));
     DevStats st;
     PIC_CUDA_TRY(cudaMemcpy(&st, c->dstats, sizeof(st), cudaMemcpyDeviceToHost));
+    c->qn_uniform = (n > 0 && st.q_mixed == 0 && st.q_first != 0.0f && std::isfinite(st.q_first)) ? st.q_first : 0.0f;
     if (st.order_breaks == 0) {
         // already in cell order: offsets make it usable by the tiled kernel without a sort
         PIC_TRY(ensure_sort_scratch(c));
@@ -623,6 +636,12 @@ int pic_gpu_host_free(void* p) {
 int pic_gpu_is_sorted(pic_ctx* c, int* out) {
     if (!c || !out) return fail(PIC_ERR_ARG, "NULL argument");
     *out = c->sorted;
+    return PIC_OK;
+}
+
+int pic_gpu_charge_uniform(pic_ctx* c, float* out) {
+    if (!c || !out) return fail(PIC_ERR_ARG, "NULL argument");
+    *out = c->qn_uniform;
     return PIC_OK;
 }
 

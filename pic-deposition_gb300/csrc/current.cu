@@ -40,6 +40,7 @@ struct JArgs {
     size_t n;
     int Nx, Ny;
     float dtdx, dtdy;
+    float qc;  // nonzero: every particle's stored charge (the charge stream is not read)
     unsigned long long *jx, *jy;
     DevStats* st;
 };
@@ -207,7 +208,7 @@ __global__ void __launch_bounds__(J_THREADS) deposit_current(JArgs a) {
             yr = __ldcs(reinterpret_cast<const float4*>(a.yr + p0));
             vx = __ldcs(reinterpret_cast<const float4*>(a.vx + p0));
             vy = __ldcs(reinterpret_cast<const float4*>(a.vy + p0));
-            q = __ldcs(reinterpret_cast<const float4*>(a.q + p0));
+            q = a.qc != 0.0f ? make_float4(a.qc, a.qc, a.qc, a.qc) : __ldcs(reinterpret_cast<const float4*>(a.q + p0));
         }
         uint32_t ckey = J_NO_CELL;
         int acc[NJ];
@@ -301,6 +302,7 @@ int deposit_current_async(pic_ctx* c, double dt) {
     a.Ny = c->Ny;
     a.dtdx = (float)(dt / c->dx);
     a.dtdy = (float)(dt / c->dy);
+    a.qc = c->qn_uniform;
     a.jx = reinterpret_cast<unsigned long long*>(c->accjx);
     a.jy = reinterpret_cast<unsigned long long*>(c->accjy);
     a.st = c->dstats;

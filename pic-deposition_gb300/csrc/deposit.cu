@@ -86,6 +86,7 @@ struct DepArgs {
     int Nx, Ny;
     float dtf, dtdx, dtdy;
     int tile_w, tile_h, tiles_x;
+    float qc;  // nonzero: every particle's stored charge (the charge stream is not read)
     DevStats* st;
 };
 
@@ -314,7 +315,7 @@ template <int S>
 __device__ __forceinline__ bool particle_values(const DepArgs& a, size_t p, int ix, int iy,
                                                 int (&val)[Frame<S>::V]) {
     const float rx = __ldcs(a.xr + p), ry = __ldcs(a.yr + p);
-    const float qn = __ldcs(a.q + p);
+    const float qn = a.qc != 0.0f ? a.qc : __ldcs(a.q + p);
     float vxx = 0.0f, vyy = 0.0f;
     if constexpr (S == S_ESK) {
         vxx = __ldcs(a.vx + p);
@@ -342,7 +343,7 @@ __device__ __forceinline__ void load_quad(const DepArgs& a, uint32_t p0, bool ok
         d.cell = __ldcs(reinterpret_cast<const uint4*>(a.cell + p0));
         d.xr = __ldcs(reinterpret_cast<const float4*>(a.xr + p0));
         d.yr = __ldcs(reinterpret_cast<const float4*>(a.yr + p0));
-        d.q = __ldcs(reinterpret_cast<const float4*>(a.q + p0));
+        d.q = a.qc != 0.0f ? make_float4(a.qc, a.qc, a.qc, a.qc) : __ldcs(reinterpret_cast<const float4*>(a.q + p0));
         if constexpr (S == S_ESK) {
             d.vx = __ldcs(reinterpret_cast<const float4*>(a.vx + p0));
             d.vy = __ldcs(reinterpret_cast<const float4*>(a.vy + p0));
@@ -664,9 +665,10 @@ __device__ __forceinline__ void particle_to_global(const DepArgs& a, uint32_t ke
 //    particles (|v| < 2^29). Denser tiles add their runs straight to the
 //    global int64 grid.
 // At the end the tile is added to the global int64 grid once.
-template <int S>
+// cell, xr, yr, q (not when uniform) (, vx, vy)
+template <int S, bool QC>
 struct StageFields {
-    static constexpr int NF = (S == S_ESK) ? 6 : 4;  // cell, xr, yr, q (, vx, vy)
+    static constexpr int NF = (S == S_ESK ? 6 : 4) - (QC ? 1 : 0);
 };
 
 constexpr int TILE_SPLIT = 15;
@@ -686,20 +688,21 @@ __device__ __forceinline__ int stage_slot(int Q) {
 // Shared memory: [alignment pad][stage buffers: NW warps x 2 x NF fields x
 // LPP*128 bytes, 1024-byte aligned][lanes' previous-run sums: NW x NV x 32
 // words, [entry][lane]][tile accumulators].
-template <int S, int LPP, int NW>
+template <int S, int LPP, int NW, bool QC>
 __host__ __device__ constexpr size_t tiled_stage_bytes() {
-    return (size_t)NW * 2 * StageFields<S>::NF * (32 * LPP) * 4;
+    return (size_t)NW * 2 * StageFields<S, QC>::NF * (32 * LPP) * 4;
 }
-template <int S, int LPP, int NW>
+template <int S, int LPP, int NW, bool QC>
 __host__ __device__ constexpr size_t tiled_fixed_bytes() {
-    return 1024 + tiled_stage_bytes<S, LPP, NW>() + (size_t)NW * 32 * 4 * Frame<S>::NX * Frame<S>::NX;
+    return 1024 + tiled_stage_bytes<S, LPP, NW, QC>() + (size_t)NW * 32 * 4 * Frame<S>::NX * Frame<S>::NX;
 }
 
-template <int S, int LPP, int NW, int MINB>
+template <int S, int LPP, int NW, int MINB, bool QC>
 __global__ void __launch_bounds__(NW * 32, MINB) deposit_tiled(DepArgs a) {
     constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
     constexpr int NV = NX * NX;
-    constexpr int NF = StageFields<S>::NF;
+    constexpr int NF = StageFields<S, QC>::NF;
+    constexpr int FV = QC ? 3 : 4;  // stage field of vx (ESK)
     constexpr int QL = LPP / 4;          // quads per lane per stage
     constexpr int STAGE = 32 * LPP;      // particles per stage
     constexpr int FB = STAGE * 4;        // bytes per field per stage buffer
@@ -716,8 +719,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_tiled(DepArgs a) {
     unsigned char* sstage = smem_raw + ((1024u - (sraw & 1023u)) & 1023u);  // 1024-byte aligned
     unsigned char* swarp = sstage + (size_t)warp * 2 * NF * FB;
     const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(swarp);
-    uint32_t* prv = reinterpret_cast<uint32_t*>(sstage + tiled_stage_bytes<S, LPP, NW>()) + warp * 32 * NV + lane;
-    uint32_t* slo = reinterpret_cast<uint32_t*>(smem_raw + tiled_fixed_bytes<S, LPP, NW>());
+    uint32_t* prv = reinterpret_cast<uint32_t*>(sstage + tiled_stage_bytes<S, LPP, NW, QC>()) + warp * 32 * NV + lane;
+    uint32_t* slo = reinterpret_cast<uint32_t*>(smem_raw + tiled_fixed_bytes<S, LPP, NW, QC>());
     int* shi = reinterpret_cast<int*>(slo + nloc);
     if (threadIdx.x == 0) s_count = 0;
     for (int i = threadIdx.x; i < nloc; i += NW * 32) {
@@ -736,10 +739,10 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_tiled(DepArgs a) {
     fptr[0] = a.cell;
     fptr[1] = a.xr;
     fptr[2] = a.yr;
-    fptr[3] = a.q;
-    if constexpr (NF == 6) {
-        fptr[4] = a.vx;
-        fptr[5] = a.vy;
+    if constexpr (!QC) fptr[3] = a.q;
+    if constexpr (S == S_ESK) {
+        fptr[FV] = a.vx;
+        fptr[FV + 1] = a.vy;
     }
     // tile row r: first particle, end, aligned start, stages
     struct Slice {
@@ -855,10 +858,13 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_tiled(DepArgs a) {
             d.cell = *reinterpret_cast<const uint4*>(sb + 0 * FB + off);
             d.xr = *reinterpret_cast<const float4*>(sb + 1 * FB + off);
             d.yr = *reinterpret_cast<const float4*>(sb + 2 * FB + off);
-            d.q = *reinterpret_cast<const float4*>(sb + 3 * FB + off);
-            if constexpr (NF == 6) {
-                d.vx = *reinterpret_cast<const float4*>(sb + 4 * FB + off);
-                d.vy = *reinterpret_cast<const float4*>(sb + 5 * FB + off);
+            if constexpr (QC)
+                d.q = make_float4(a.qc, a.qc, a.qc, a.qc);
+            else
+                d.q = *reinterpret_cast<const float4*>(sb + 3 * FB + off);
+            if constexpr (S == S_ESK) {
+                d.vx = *reinterpret_cast<const float4*>(sb + FV * FB + off);
+                d.vy = *reinterpret_cast<const float4*>(sb + (FV + 1) * FB + off);
             }
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -1009,17 +1015,18 @@ __global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double
     if (i < g) rho[i] = __dadd_rn(__dmul_rn((double)acc[i], unit), background);
 }
 
-template <int S, int LPP, int NW, int MINB>
+template <int S, int LPP, int NW, int MINB, bool QC>
 static void launch_tiled(pic_ctx* c, const DepArgs& a, unsigned tiles) {
     const size_t smem =
-        tiled_fixed_bytes<S, LPP, NW>() + (size_t)(a.tile_h + 3) * (a.tile_w + 3) * 2 * sizeof(uint32_t);
+        tiled_fixed_bytes<S, LPP, NW, QC>() + (size_t)(a.tile_h + 3) * (a.tile_w + 3) * 2 * sizeof(uint32_t);
     // dynamic shared memory above 48 KB must be opted into (once per kernel)
     static size_t opted = 0;
     if (smem > opted) {
-        cudaFuncSetAttribute(deposit_tiled<S, LPP, NW, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(deposit_tiled<S, LPP, NW, MINB, QC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
         opted = smem;
     }
-    deposit_tiled<S, LPP, NW, MINB><<<tiles, NW * 32, smem, c->stream>>>(a);
+    deposit_tiled<S, LPP, NW, MINB, QC><<<tiles, NW * 32, smem, c->stream>>>(a);
 }
 
 template <int S>
@@ -1032,7 +1039,10 @@ static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
         // registers (5 CTAs per SM), measured fastest at 1024^2 x 64 particles/cell.
         // cp.async staging measured 10 % faster than TMA tensor copies of the
         // same stages (128-byte swizzle, one lane issuing, mbarrier completion)
-        launch_tiled<S, 8, 4, S == S_TSC ? 5 : 4>(c, a, tiles);
+        if (a.qc != 0.0f)  // one charge for all particles: the charge stream is not staged
+            launch_tiled<S, 8, 4, S == S_TSC ? 5 : 4, true>(c, a, tiles);
+        else
+            launch_tiled<S, 8, 4, S == S_TSC ? 5 : 4, false>(c, a, tiles);
         prof_end(c);
         return check_launch(c, "deposit_tiled");
     }
@@ -1106,6 +1116,7 @@ int deposit_rho(pic_ctx* c, int scheme, double dt, double background) {
     a.tile_w = c->tile_w;
     a.tile_h = c->tile_h;
     a.tiles_x = (c->Nx + c->tile_w - 1) / c->tile_w;
+    a.qc = c->qn_uniform;
     a.st = c->dstats;
     if (c->n > 0) {
         switch (scheme) {

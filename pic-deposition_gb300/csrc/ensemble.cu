@@ -981,6 +981,7 @@ int pic_ens_create(const pic_ens_member* runs_in, int nruns, const pic_ens_confi
         c->sorted = 0;
         c->part_valid = 0;
         c->qsum_valid = 0;
+        c->qn_uniform = -1.0f;
     }
     // batched FFT plans per grid size
     size_t spec_total = 0;

@@ -136,6 +136,7 @@ extern "C" int pic_gpu_generate(pic_ctx* c, const pic_gen_config* g) {
     c->sorted = 0;
     c->part_valid = 0;
     c->qsum_valid = 0;
+    c->qn_uniform = g->n ? a.qn : 0.0f;
     c->launches++;
     return pic_gpu_synchronize(c);
 }

@@ -22,7 +22,8 @@ struct DevStats {
     int err;
     unsigned int err_info;
     unsigned int order_breaks;  // uploads: count of i with cell[i] < cell[i-1]
-    unsigned int pad[2];
+    unsigned int q_mixed;       // uploads: nonzero when the stored charges differ
+    float q_first;              // uploads: the first particle's stored charge
 };
 
 enum DevErr : int {
@@ -61,6 +62,11 @@ struct pic_ctx {
     uint32_t* cell = nullptr;
     float *xr = nullptr, *yr = nullptr, *vx = nullptr, *vy = nullptr, *q = nullptr, *m = nullptr;
     int has_mass = 0;
+    // Nonzero when every particle's stored charge q/max|q| equals it (one
+    // species; set by an upload that finds it so, and by a generate): the
+    // kernels then use the value instead of reading the charge stream (the
+    // array stays valid, the sort leaves it in place).
+    float qn_uniform = 0.0f;
     int sorted = 0;  // particles are in stable cell order and `offsets` is valid
     // `offsets` (from the last sort) still cut the particle array into the cells'
     // ranges of that sort: kept by the push, which moves particles without

@@ -31,6 +31,7 @@ struct MoveArgs {
     size_t n;
     int Nx, Ny;
     float dtf, dtdx, dtdy;
+    float qc;  // nonzero: every particle's stored charge (the charge stream is not read)
     const DevStats* st;
 };
 
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(256) move_particles(MoveArgs a) {
             const size_t i01 = (size_t)iyp * a.Nx + ix, i11 = (size_t)iyp * a.Nx + ixp;
             const float ex = interp(a.Exf, i00, i10, i01, i11, rx, ry);
             const float ey = interp(a.Eyf, i00, i10, i01, i11, rx, ry);
-            const float qf = a.q[p] * maxq;
+            const float qf = (a.qc != 0.0f ? a.qc : a.q[p]) * maxq;
             const float coef = a.m ? __fdiv_rn(-qf, a.m[p]) : -qf;
             vxx = vxx + (coef * ex) * a.dtf;
             vyy = vyy + (coef * ey) * a.dtf;
@@ -100,6 +101,7 @@ int move(pic_ctx* c, double dt, bool gather, bool push) {
     a.dtf = (float)dt;
     a.dtdx = (float)(dt / c->dx);
     a.dtdy = (float)(dt / c->dy);
+    a.qc = c->qn_uniform;
     a.st = c->dstats;
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);

@@ -277,16 +277,21 @@ int sort_particles(pic_ctx* c) {
     GatherArgs g;
     g.perm = c->idx_a;
     g.n = n;
-    float* cur[6] = {c->xr, c->yr, c->vx, c->vy, c->q, c->m};
-    g.count = c->has_mass ? 6 : 5;
-    for (int k = 0; k < 6; ++k) {
-        g.src[k] = cur[k];
-        g.dst[k] = c->alt[k];
+    // the payload: offsets, velocities, charges (not when uniform: any order of
+    // equal values is the same array) and masses (when stored)
+    float** slots[6] = {&c->xr, &c->yr, &c->vx, &c->vy, &c->q, &c->m};
+    int fields[6], nf = 0;
+    for (int k = 0; k < 6; ++k)
+        if ((k != 4 || c->qn_uniform == 0.0f) && (k != 5 || c->has_mass)) fields[nf++] = k;
+    g.count = nf;
+    for (int j = 0; j < nf; ++j) {
+        g.src[j] = *slots[fields[j]];
+        g.dst[j] = c->alt[fields[j]];
     }
     gather_payload<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(g);
     PIC_TRY(check_launch(c, "gather_payload"));
-    float** slots[6] = {&c->xr, &c->yr, &c->vx, &c->vy, &c->q, &c->m};
-    for (int k = 0; k < g.count; ++k) {
+    for (int j = 0; j < nf; ++j) {
+        const int k = fields[j];
         float* t = *slots[k];
         *slots[k] = c->alt[k];
         c->alt[k] = t;

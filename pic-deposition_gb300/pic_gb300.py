@@ -72,6 +72,7 @@ _SIGS = [
     ("pic_gpu_get_rho_fixed", [_vp, _vp, _dp]),
     ("pic_gpu_get_rho", [_vp, _vp]),
     ("pic_gpu_is_sorted", [_vp, C.POINTER(C.c_int)]),
+    ("pic_gpu_charge_uniform", [_vp, C.POINTER(C.c_float)]),
     ("pic_gpu_profile_enable", [_vp, C.c_int]),
     ("pic_gpu_profile_read", [_vp, C.c_char_p, _dp, C.POINTER(C.c_longlong)]),
     ("pic_gpu_host_alloc", [C.c_size_t, C.POINTER(_vp)]),
@@ -396,6 +397,12 @@ class Context:
         v = C.c_int()
         _check(lib().pic_gpu_is_sorted(self.h, C.byref(v)))
         return bool(v.value)
+
+    def charge_uniform(self) -> float:
+        """The stored charge q/max|q| shared by every particle (+-1), 0.0 when they differ."""
+        v = C.c_float()
+        _check(lib().pic_gpu_charge_uniform(self.h, C.byref(v)))
+        return v.value
 
     def profile(self, enable: bool = True):
         _check(lib().pic_gpu_profile_enable(self.h, int(enable)))

@@ -173,6 +173,29 @@ def test_pushed_since_sort_uses_stale_ranges(port, pg, scheme):
     assert np.array_equal(acc, want) and np.array_equal(acc_s, want) and np.array_equal(acc_u, want)
 
 
+@pytest.mark.parametrize("scheme", [NGP, CIC, TSC, ESK])
+def test_uniform_charge_skips_the_charge_stream(port, pg, scheme):
+    """One charge for every particle is detected at upload (the kernels then do not
+    read the charge stream, and the sort leaves the charge array in place); mixed
+    charges are read per particle. Both give the oracle's grid bit for bit."""
+    base = maxwellian(port, 48, 40, 4.8, 4.0, 30000, seed=31, T=0.4)
+    for q, want_uniform in ((np.full(30000, -2.5), -1.0), (np.full(30000, 0.75), 1.0),
+                            (np.where(np.arange(30000) % 7 == 0, 1.0, -1.0), 0.0)):
+        p = dict(base, q=q)
+        with pg.Context(48, 40, 4.8, 4.0, len(q)) as c:
+            c.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+            assert c.charge_uniform() == want_uniform
+            c.sort()
+            lay = c.device_layout()
+            if want_uniform:
+                assert np.all(lay["q"] == np.float32(want_uniform))
+        check(port, pg, 48, 40, 4.8, 4.0, p, scheme, 0.03, "sorted")
+        check(port, pg, 48, 40, 4.8, 4.0, p, scheme, 0.03, "unsorted")
+    with pg.Context(16, 16, 16.0, 16.0, 1000) as c:
+        c.generate(1000, vth=0.1, charge=-0.5, seed=3)
+        assert c.charge_uniform() == -1.0
+
+
 # ---- edge cases ------------------------------------------------------------
 @pytest.mark.parametrize("scheme", [NGP, CIC, TSC, ESK])
 @pytest.mark.parametrize("order", ["sorted", "unsorted"])
