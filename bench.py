@@ -15,9 +15,10 @@ needed between steps.
           summed over ranks (replicas; one GPU each), max time over ranks.
   e2e     the same metric through the public C ABI with host buffers: every
           step uploads x, y, q (FP64, pinned) and downloads rho (FP64).
-  roofline  the deposit kernel alone: algorithmic bytes (16 B per particle +
-          8 B per cell) / its mean CUDA-event duration, against the measured
-          HBM copy bandwidth in MEASURED_PEAKS.json.
+  roofline  the deposit kernel alone: algorithmic bytes (12 B per particle
+          when every particle has the same charge, as here -- the charge stream
+          is not read -- else 16 B; + 8 B per cell) / its mean CUDA-event
+          duration, against the measured HBM copy bandwidth in MEASURED_PEAKS.json.
   cpu_baseline  the reference's FP64 CPU deposit on the host cores (rank 0).
 
 --impl reference times the reference's own CPU path (oracle/_ref when it loads
