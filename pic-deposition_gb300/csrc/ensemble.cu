@@ -195,7 +195,7 @@ __device__ __forceinline__ void load_quad4(const StepArgs& a, size_t p0, bool ok
         d.cell = __ldcs(reinterpret_cast<const uint4*>(a.cell + p0));
         d.xr = __ldcs(reinterpret_cast<const float4*>(a.xr + p0));
         d.yr = __ldcs(reinterpret_cast<const float4*>(a.yr + p0));
-        d.q = __ldcs(reinterpret_cast<const float4*>(a.q + p0));
+        d.q = make_float4(-1.0f, -1.0f, -1.0f, -1.0f);  // every stored charge is -1 (ens_init_run)
     }
 }
 
