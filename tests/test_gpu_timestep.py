@@ -87,6 +87,27 @@ def test_conservation_study_setup(pg, port, scheme):
     assert abs(drift) <= 1e-4, drift
 
 
+def test_kinetic_sum_and_charge_cache(pg, port):
+    """The kinetic diagnostic (double-FP32 per thread, FP64 across threads) agrees
+    with an FP64 sum over the device's FP32 velocities to 1e-13; the total charge,
+    summed once per particle set, follows a new upload of different charges."""
+    p = port.init_particles(0, 32, 32, 1.0, 1.0, 50000, p0=2.0, seed=8)
+    with start(pg, 32, 32, 1.0, 1.0, p) as c:
+        c.deposit(CIC, 0.0, download=False)
+        c.poisson_fft()
+        d = c.diagnostics()
+        lay = c.device_layout()
+        ke = 0.5 * np.sum(lay["vx"].astype(np.float64) ** 2 + lay["vy"].astype(np.float64) ** 2)
+        assert abs(d["kinetic_energy"] - ke) <= 1e-13 * ke
+        assert d["total_charge"] == pytest.approx(np.sum(p["q"]), rel=1e-6)
+        h = c.run(3, scheme=CIC, dt=0.002)
+        q2 = np.where(np.arange(len(p["q"])) % 3 == 0, 2.0, -1.0) * abs(p["q"][0])
+        c.upload(p["x"], p["y"], q2, p["vx"], p["vy"], p["m"])
+        h2 = c.run(3, scheme=CIC, dt=0.002)
+    assert h[0, 1] == pytest.approx(np.sum(p["q"]), rel=1e-6)
+    assert h2[0, 1] == pytest.approx(np.sum(q2), rel=1e-6) and h2[0, 1] != h[0, 1]
+
+
 def test_rbgs_matches_oracle(pg, port):
     nx, ny = 64, 48
     rng = np.random.default_rng(0)
