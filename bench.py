@@ -383,8 +383,10 @@ def run_gpu(args, d: Dist):
     for _ in range(10):
         ctx.gather_push(0.0)
     ms, cnt = ctx.profile_read("gather_push")
+    # reads cell, xr, yr, vx, vy (+ q when charges differ), writes cell, xr, yr, vx, vy; FP32 Ex, Ey
+    gp_bpp = 40 + (0 if q_uniform else 4)
     extras["gather_push"] = {"particles_per_s": n / (ms / cnt / 1e3), "kernel_ms": ms / cnt,
-                             "kernel_gbs": (44 * n + 8 * G) / (ms / cnt / 1e3) / 1e9}
+                             "kernel_gbs": (gp_bpp * n + 8 * G) / (ms / cnt / 1e3) / 1e9}
     # full time step: push, [sort every 10], TSC deposit + background, FFT Poisson,
     # gather, FP64 diagnostics; CUDA-graph replay; host wall time per step
     ctx.run(3, scheme=SCHEMES["TSC"], dt=ESK_DT, background=float(PPC), sort_interval=10, use_graph=True)
