@@ -390,10 +390,9 @@ __device__ __forceinline__ void flush_global_nd(const DepArgs& a, uint32_t key, 
     }
 }
 
-// Any-order path with run aggregation: the sorted path's warp step (4
-// consecutive particles per lane, register sums per cell, segmented warp scan)
-// over the whole particle array, with the run totals added straight to the
-// global int64 grid. It needs no per-cell offsets and is correct for any order;
+// Any-order path with run aggregation: a warp step of 128 consecutive particles
+// (4 per lane, register sums per cell, segmented warp scan) over the whole
+// particle array, with the run totals added straight to the global int64 grid. It needs no per-cell offsets and is correct for any order;
 // runs are long when the particles are nearly cell-ordered, as between the
 // sorts of a time-stepping loop.
 template <int S>
