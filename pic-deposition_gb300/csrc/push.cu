@@ -53,12 +53,32 @@ template <bool GATHER, bool PUSH>
 __global__ void __launch_bounds__(256) move_particles(MoveArgs a) {
     const float maxq = load_maxq(a.st);
     const float inv_nx = 1.0f / (float)a.Nx;
-    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += (size_t)gridDim.x * blockDim.x) {
-        const uint32_t key = a.cell[p];
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    // the next particle's key, offsets and velocities are loaded before this one is
+    // used: only the field gather's round trip stays on the critical path
+    size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t key = 0;
+    float rx = 0.0f, ry = 0.0f, vxx = 0.0f, vyy = 0.0f;
+    if (p < a.n) {
+        key = a.cell[p];
+        rx = a.xr[p];
+        ry = a.yr[p];
+        vxx = a.vx[p];
+        vyy = a.vy[p];
+    }
+    for (; p < a.n; p += stride) {
+        const size_t pn = p + stride;
+        uint32_t nkey = 0;
+        float nrx = 0.0f, nry = 0.0f, nvx = 0.0f, nvy = 0.0f;
+        if (pn < a.n) {
+            nkey = a.cell[pn];
+            nrx = a.xr[pn];
+            nry = a.yr[pn];
+            nvx = a.vx[pn];
+            nvy = a.vy[pn];
+        }
         int iy, ix;
         split_key(key, a.Nx, inv_nx, iy, ix);
-        float rx = a.xr[p], ry = a.yr[p];
-        float vxx = a.vx[p], vyy = a.vy[p];
         if constexpr (GATHER) {
             const int ixp = ix + 1 == a.Nx ? 0 : ix + 1, iyp = iy + 1 == a.Ny ? 0 : iy + 1;
             const size_t i00 = (size_t)iy * a.Nx + ix, i10 = (size_t)iy * a.Nx + ixp;
@@ -79,6 +99,11 @@ __global__ void __launch_bounds__(256) move_particles(MoveArgs a) {
             a.yr[p] = ry;
             a.cell[p] = (uint32_t)iy * (uint32_t)a.Nx + (uint32_t)ix;
         }
+        key = nkey;
+        rx = nrx;
+        ry = nry;
+        vxx = nvx;
+        vyy = nvy;
     }
 }
 
