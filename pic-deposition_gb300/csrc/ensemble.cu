@@ -200,7 +200,7 @@ __device__ __forceinline__ void load_quad4(const StepArgs& a, size_t p0, bool ok
 }
 
 // The step's particle work in one launch (see the file header).
-__global__ void __launch_bounds__(ENS_THREADS) ens_step_kernel(StepArgs a) {
+__global__ void __launch_bounds__(ENS_THREADS, 4) ens_step_kernel(StepArgs a) {
     __shared__ uint32_t pbase[MAX_RUNS], cbase[MAX_RUNS];
     for (int i = threadIdx.x; i < a.nruns; i += ENS_THREADS) {
         pbase[i] = a.runs[i].pbase;
@@ -216,9 +216,14 @@ __global__ void __launch_bounds__(ENS_THREADS) ens_step_kernel(StepArgs a) {
             const int N = r.N;
             const size_t b0 = r.cell_base;
             const size_t nq = r.np / 4, q0 = r.pbase / 4;  // particle counts and bases are multiples of 4
+            // the next quad's cell keys are loaded before this quad is used, so its
+            // field gathers can start with the other fields' loads
+            uint4 ncl = make_uint4(0, 0, 0, 0);
+            if (tid < nq) ncl = *reinterpret_cast<const uint4*>(a.cell + (q0 + tid) * 4);
             for (size_t qi = tid; qi < nq; qi += nthreads) {
                 const size_t p0 = (q0 + qi) * 4;
-                uint4 cl = *reinterpret_cast<const uint4*>(a.cell + p0);
+                uint4 cl = ncl;
+                if (qi + nthreads < nq) ncl = *reinterpret_cast<const uint4*>(a.cell + (q0 + qi + nthreads) * 4);
                 float4 fx = *reinterpret_cast<const float4*>(a.xr + p0);
                 float4 fy = *reinterpret_cast<const float4*>(a.yr + p0);
                 float4 gx = *reinterpret_cast<const float4*>(a.vx + p0);
