@@ -3,8 +3,8 @@
 // PoissonSolverGS::solve (src/pic/poisson_gs.cpp:11-61) is lexicographic,
 // zeroes phi on every call and stops on max|dphi| < 1e-6. This solver keeps its
 // 5-point stencil and sign, phi = ((phiW+phiE)/dx^2 + (phiS+phiN)/dy^2 + rho*dV)
-// / (2(1/dx^2+1/dy^2)) (poisson_gs.cpp:32-38), and changes what the benchmark spec
-// asks for: red-black ordering (all points with (i+j) even, then odd; each
+// / (2(1/dx^2+1/dy^2)) (poisson_gs.cpp:32-38), and changes what a data-parallel
+// solve with a learned warm start needs: red-black ordering (all points with (i+j) even, then odd; each
 // colour is one data-parallel kernel), the right-hand side rho*dV with its mean
 // removed (the periodic problem is singular), a warm start from the phi already
 // in the context (the previous step's, or a learned guess), and the stop

@@ -16,7 +16,7 @@ for p in (ORACLE, PKG):
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the kernels through the C ABI)")
-    config.addinivalue_line("markers", "slow: full-size (BASELINE-shape) case")
+    config.addinivalue_line("markers", "slow: full-size (benchmark-shape) case")
 
 
 @pytest.fixture(scope="session")
