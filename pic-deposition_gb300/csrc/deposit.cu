@@ -324,10 +324,6 @@ __device__ __forceinline__ bool particle_values(const DepArgs& a, size_t p, int 
     return stencil_values<S>(a, rx, ry, qn, vxx, vyy, ix, iy, p, val);
 }
 
-__device__ __forceinline__ void sadd(long long* s, int idx, int v) {
-    atomicAdd(reinterpret_cast<unsigned long long*>(s + idx), (unsigned long long)(long long)v);
-}
-
 constexpr uint32_t NO_CELL = 0xffffffffu;
 
 // Four consecutive particles of each field, one 128-bit streaming load per field.
