@@ -132,12 +132,17 @@ def nn_conv3x3(op: int, x: np.ndarray, weight=None, bias=None, aux=None, cin: in
     (9, cout, cin), bias FP32 (cout,). Returns BF16 bits (B, H, W, C) for ops 0
     and 2, FP32 (B, H, W) for op 1 and (dw (9, cout, cin), db (cout,)) for op 3.
     """
-    B, H, W = x.shape[:3]
-    x = np.ascontiguousarray(x, dtype=np.uint16)
+    if np.ndim(x) < 3:
+        raise ValueError("x: expected (B, H, W, C)")
+    B, H, W = np.shape(x)[:3]
+    px = B * H * W
+    # channels of x and aux per op (the C side reads these sizes through plain pointers)
+    xc, ac = {NN_FWD_RELU: (cin, 0), NN_FWD_OUT: (cin, 0), NN_DGRAD: (cout, cin), NN_WGRAD: (cin, cout)}.get(op, (cin, 0))
+    x = _sized(x, np.uint16, px * xc, "x")
     ptr = lambda a: None if a is None else a.ctypes.data_as(_vp)
-    w = None if weight is None else np.ascontiguousarray(weight, dtype=np.float32)
-    b = None if bias is None else np.ascontiguousarray(bias, dtype=np.float32)
-    a = None if aux is None else np.ascontiguousarray(aux, dtype=np.uint16)
+    w = None if op == NN_WGRAD else _sized(weight, np.float32, 9 * cout * cin, "weight")
+    b = _sized(bias, np.float32, cout, "bias") if op in (NN_FWD_RELU, NN_FWD_OUT) else None
+    a = _sized(aux, np.uint16, px * ac, "aux") if ac else None
     if op == NN_FWD_RELU:
         out = np.zeros((B, H, W, cout), np.uint16)
     elif op == NN_FWD_OUT:
@@ -306,6 +311,17 @@ def _arr(a, dt):
     return None if a is None else np.ascontiguousarray(a, dtype=dt)
 
 
+def _sized(a, dt, n: int, what: str):
+    """Contiguous `dt` copy of `a` that holds exactly n values (the C side reads n through a
+    plain pointer, so a shorter array would be read past its end); None stays None."""
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=dt)
+    if a.size != n:
+        raise ValueError(f"{what}: expected {n} values, got {a.size}")
+    return a
+
+
 class Context:
     """Device-resident particles and grid on one GPU (C ABI pic_ctx)."""
 
@@ -337,8 +353,8 @@ class Context:
 
     # ---- particles ----
     def upload(self, x, y, q, vx=None, vy=None, m=None):
-        arrs = [_arr(a, np.float64) for a in (x, y, vx, vy, q, m)]
-        n = len(arrs[0])
+        n = int(np.size(x))
+        arrs = [_sized(a, np.float64, n, name) for a, name in zip((x, y, vx, vy, q, m), ("x", "y", "vx", "vy", "q", "m"))]
         self._keep = arrs
         _check(lib().pic_gpu_upload_particles(self.h, *[_ptr(a) for a in arrs], n))
         self.n = n
@@ -416,11 +432,11 @@ class Context:
 
     # ---- fields / Poisson / motion / diagnostics ----
     def set_rho(self, rho):
-        r = _arr(rho, np.float64)
+        r = _sized(rho, np.float64, self.G, "rho")
         _check(lib().pic_gpu_set_rho(self.h, _ptr(r)))
 
     def set_fields(self, phi=None, ex=None, ey=None):
-        a = [_arr(v, np.float64) for v in (phi, ex, ey)]
+        a = [_sized(v, np.float64, self.G, name) for v, name in zip((phi, ex, ey), ("phi", "ex", "ey"))]
         _check(lib().pic_gpu_set_fields(self.h, *[_ptr(v) for v in a]))
 
     def fields(self):
@@ -500,19 +516,21 @@ class Context:
         return loss[:epochs]
 
     def ws_loss_grad(self, inputs, targets):
-        inputs = _arr(inputs, np.float32)
-        targets = _arr(targets, np.float32)
+        inputs = np.asarray(inputs)
+        batch = int(inputs.shape[0]) if inputs.ndim > 1 else 1
+        inputs = _sized(inputs, np.float32, batch * self.G, "inputs")
+        targets = _sized(targets, np.float32, batch * self.G, "targets")
         grad = np.zeros(self.ws_param_count(), np.float32)
         loss = C.c_double()
-        _check(lib().pic_gpu_ws_loss_grad(self.h, inputs.shape[0], _ptr(inputs), _ptr(targets), C.byref(loss),
-                                          _ptr(grad)))
+        _check(lib().pic_gpu_ws_loss_grad(self.h, batch, _ptr(inputs), _ptr(targets), C.byref(loss), _ptr(grad)))
         return loss.value, grad
 
     def ws_predict(self, field):
-        field = _arr(field, np.float32)
+        shape = np.shape(field)
+        field = _sized(field, np.float32, self.G, "field")
         out = np.zeros(field.size, np.float32)
         _check(lib().pic_gpu_ws_predict(self.h, _ptr(field), _ptr(out)))
-        return out.reshape(field.shape)
+        return out.reshape(shape)
 
     def ws_study(self, steps, dt, background=0.0, sort_interval=20, tol=1e-8, check_every=16,
                  max_iters=2_000_000) -> dict:
