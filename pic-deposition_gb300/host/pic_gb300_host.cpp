@@ -53,7 +53,23 @@ pic_ctx* context_for(const Domain& d, std::size_t n) {
     return h;
 }
 
+// The C ABI reads the particle count through every particle pointer and Nx*Ny
+// values through every grid pointer; the vectors behind them are resizable, so
+// their sizes are checked here (std::runtime_error, the reference's convention).
+void check_particles(const ParticlesSoA& p) {
+    const std::size_t n = p.size();
+    if (p.y().size() != n || p.vx().size() != n || p.vy().size() != n || p.q().size() != n || p.m().size() != n)
+        throw std::runtime_error("ParticlesSoA: x, y, vx, vy, q and m differ in length");
+}
+
+void check_grid(const FieldGrid& g, const Domain& d) {
+    const std::size_t cells = static_cast<std::size_t>(d.Nx) * static_cast<std::size_t>(d.Ny);
+    if (g.rho().size() != cells || g.phi().size() != cells || g.Ex().size() != cells || g.Ey().size() != cells)
+        throw std::runtime_error("FieldGrid: rho, phi, Ex and Ey must hold Nx*Ny values of the domain");
+}
+
 void upload(pic_ctx* h, const ParticlesSoA& p) {
+    check_particles(p);
     check(pic_gpu_upload_particles(h, p.x().data(), p.y().data(), p.vx().data(), p.vy().data(), p.q().data(),
                                    p.m().data(), p.size()));
 }
@@ -217,6 +233,8 @@ DepositionStats estimateBytes(const DepositionConfig& config, std::size_t num_pa
 
 void depositChargeSoA(const ParticlesSoA& particles, FieldGrid& grid, const DepositionConfig& config) {
     require_gb300(config);
+    check_particles(particles);
+    check_grid(grid, grid.domain());
     grid.clearRho();
     pic_ctx* h = context_for(grid.domain(), particles.size());
     upload(h, particles);
@@ -227,6 +245,8 @@ void depositChargeSoA(const ParticlesSoA& particles, FieldGrid& grid, const Depo
 DepositionStats depositChargeTimedSoA(const ParticlesSoA& particles, FieldGrid& grid, const DepositionConfig& config,
                                       int repeats) {
     require_gb300(config);
+    check_particles(particles);
+    check_grid(grid, grid.domain());
     using Clock = std::chrono::steady_clock;
     pic_ctx* h = context_for(grid.domain(), particles.size());
     upload(h, particles);
@@ -268,6 +288,8 @@ DepositionStats depositChargeTimedSoA(const ParticlesSoA& particles, FieldGrid& 
 }
 
 void gatherFieldsSoA(ParticlesSoA& particles, FieldGrid& grid, double dt) {
+    check_particles(particles);
+    check_grid(grid, grid.domain());
     pic_ctx* h = context_for(grid.domain(), particles.size());
     upload(h, particles);
     check(pic_gpu_set_fields(h, nullptr, grid.Ex().data(), grid.Ey().data()));
@@ -277,6 +299,7 @@ void gatherFieldsSoA(ParticlesSoA& particles, FieldGrid& grid, double dt) {
 }
 
 void pushParticlesSoA(ParticlesSoA& particles, const FieldGrid& grid, double dt) {
+    check_particles(particles);
     pic_ctx* h = context_for(grid.domain(), particles.size());
     upload(h, particles);
     check(pic_gpu_push(h, dt));
@@ -285,6 +308,7 @@ void pushParticlesSoA(ParticlesSoA& particles, const FieldGrid& grid, double dt)
 }
 
 void sortParticlesByCell(ParticlesSoA& particles, const Domain& domain) {
+    check_particles(particles);
     const std::size_t n = particles.size();
     pic_ctx* h = context_for(domain, n);
     upload(h, particles);
@@ -358,6 +382,7 @@ DepositionBackend backendFromString(const std::string& name) {
 
 // ---- Poisson ----
 void PoissonSolverFFT::solve(FieldGrid& grid) {
+    check_grid(grid, domain_);
     pic_ctx* h = context_for(domain_, 1);
     check(pic_gpu_set_rho(h, grid.rho().data()));
     check(pic_gpu_poisson_fft(h));
@@ -365,6 +390,7 @@ void PoissonSolverFFT::solve(FieldGrid& grid) {
 }
 
 void PoissonSolverGS::solve(FieldGrid& grid) {
+    check_grid(grid, domain_);
     pic_ctx* h = context_for(domain_, 1);
     check(pic_gpu_set_rho(h, grid.rho().data()));
     check(pic_gpu_set_fields(h, grid.phi().data(), nullptr, nullptr));
@@ -417,6 +443,8 @@ Simulation::Simulation(SimulationConfig config) : config_(std::move(config)), gr
 SimulationResult Simulation::run() {
     SimulationResult r;
     const Domain& d = config_.domain;
+    check_particles(particles_);
+    check_grid(grid_, d);
     pic_ctx* h = context_for(d, particles_.size());
     upload(h, particles_);
     pic_run_config rc{};

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <functional>
 #include <iostream>
 #include <numeric>
 #include <string>
@@ -319,11 +320,57 @@ int dumpDeposit(const std::string& scheme, const std::string& out) {
     return 0;
 }
 
+// Vectors of the wrong size are rejected with std::runtime_error before any
+// device work (no GPU needed): the C ABI would read past their ends.
+bool throwsWith(const std::function<void()>& f, const std::string& what) {
+    try {
+        f();
+    } catch (const std::runtime_error& e) {
+        return std::string(e.what()).find(what) != std::string::npos;
+    }
+    return false;
+}
+
+int checkSizes() {
+    pic::Domain d;
+    d.Nx = 16;
+    d.Ny = 8;
+    d.updateDerived();
+    pic::DepositionConfig cfg;
+    bool ok = true;
+    {
+        pic::FieldGrid grid(d);
+        pic::ParticlesSoA p(10);
+        p.y().resize(9);
+        ok &= throwsWith([&] { pic::depositChargeSoA(p, grid, cfg); }, "differ in length");
+        ok &= throwsWith([&] { pic::sortParticlesByCell(p, d); }, "differ in length");
+        ok &= throwsWith([&] { pic::pushParticlesSoA(p, grid, 0.1); }, "differ in length");
+    }
+    {
+        pic::FieldGrid grid(d);
+        pic::ParticlesSoA p(10);
+        grid.rho().resize(d.Nx * d.Ny - 1);
+        ok &= throwsWith([&] { pic::depositChargeSoA(p, grid, cfg); }, "FieldGrid");
+        ok &= throwsWith([&] { pic::gatherFieldsSoA(p, grid, 0.1); }, "FieldGrid");
+    }
+    {
+        pic::Domain other = d;
+        other.Nx = 32;
+        other.updateDerived();
+        pic::FieldGrid grid(d);
+        pic::PoissonSolverFFT fft(other);
+        ok &= throwsWith([&] { fft.solve(grid); }, "FieldGrid");
+    }
+    std::printf("%s sizes\n", ok ? "PASS" : "FAIL");
+    return ok ? 0 : 1;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
     if (argc == 4 && std::string(argv[1]) == "init") return dumpInit(argv[2], argv[3]);
     if (argc == 4 && std::string(argv[1]) == "deposit") return dumpDeposit(argv[2], argv[3]);
+    if (argc == 2 && std::string(argv[1]) == "sizes") return checkSizes();
     bool ok = true;
     ok &= testSchemeChargeConservation(pic::DepositionScheme::CIC);
     ok &= testSchemeChargeConservation(pic::DepositionScheme::TSC);

@@ -58,6 +58,11 @@ def test_initialisers_match_oracle(exe, port, tmp_path, kind):
         assert np.array_equal(got[k], want[k]), k
 
 
+def test_wrong_sizes_are_rejected_before_device_work(exe):
+    r = subprocess.run([exe, "sizes"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and "PASS sizes" in r.stdout, r.stdout + r.stderr
+
+
 @pytest.mark.gpu
 def test_main_test_program(exe):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
