@@ -5,7 +5,9 @@ its own GPU, joined only by a barrier around the timed region and a max over
 ranks of the step time (no data-path collective). These tests run that host
 logic without a GPU: the barrier and the max across two gloo ranks, and the
 reference arm under torchrun, where rank 0 alone does the work and prints the
-one JSON line and the other rank exits 0 without output.
+one JSON line and the other rank exits 0 without output; and the reference
+arm's line in one process (the keys of the benchmark line, and the GB300 arm's
+metric and workload).
 """
 import json
 import os
@@ -71,3 +73,22 @@ def test_reference_arm_under_torchrun_two_ranks():
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_single_process_line_keeps_the_contract():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "3", "--warmup", "3", "--ppc",
+                        "1"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    lines = [l for l in r.stdout.splitlines() if l.strip().startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e", "impl"):
+        assert k in d, k
+    # the same metric, unit and direction as the GB300 arm, so that the two lines compare
+    assert d["metric"] == bench.METRIC and d["unit"] == "particles/s" and d["higher_is_better"] is True
+    assert d["n_gpus"] == 1 and d["config"]["workload"] == bench.WORKLOAD
+    assert d["ms_per_step"] > 0 and d["value"] > 0
