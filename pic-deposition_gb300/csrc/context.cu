@@ -1,6 +1,7 @@
 // Context lifecycle, errors, particle upload/download and the device-wide scan.
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -18,6 +19,23 @@ int fail(int code, const std::string& msg) {
 int cuda_fail(cudaError_t e, const char* what) {
     g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
     return PIC_ERR_CUDA;
+}
+
+int opt_in_dynamic_smem(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> done;
+    int dev = 0;
+    PIC_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& have = done[std::make_pair(kernel, dev)];
+    if (bytes <= have) return PIC_OK;
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return cuda_fail(e, "cudaFuncSetAttribute(MaxDynamicSharedMemorySize)");
+    }
+    have = bytes;
+    return PIC_OK;
 }
 
 int check_launch(pic_ctx* ctx, const char* what) {

@@ -1013,17 +1013,14 @@ __global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double
 }
 
 template <int S, int LPP, int NW, int MINB, bool QC>
-static void launch_tiled(pic_ctx* c, const DepArgs& a, unsigned tiles) {
+static int launch_tiled(pic_ctx* c, const DepArgs& a, unsigned tiles) {
     const size_t smem =
         tiled_fixed_bytes<S, LPP, NW, QC>() + (size_t)(a.tile_h + 3) * (a.tile_w + 3) * 2 * sizeof(uint32_t);
-    // dynamic shared memory above 48 KB must be opted into (once per kernel)
-    static size_t opted = 0;
-    if (smem > opted) {
-        cudaFuncSetAttribute(deposit_tiled<S, LPP, NW, MINB, QC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-        opted = smem;
-    }
+    // dynamic shared memory above 48 KB must be opted into
+    const int rc = opt_in_dynamic_smem((const void*)deposit_tiled<S, LPP, NW, MINB, QC>, smem);
+    if (rc != PIC_OK) return rc;
     deposit_tiled<S, LPP, NW, MINB, QC><<<tiles, NW * 32, smem, c->stream>>>(a);
+    return PIC_OK;
 }
 
 template <int S>
@@ -1036,11 +1033,13 @@ static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
         // registers (5 CTAs per SM), measured fastest at 1024^2 x 64 particles/cell.
         // cp.async staging measured 10 % faster than TMA tensor copies of the
         // same stages (128-byte swizzle, one lane issuing, mbarrier completion)
+        int rc;
         if (a.qc != 0.0f)  // one charge for all particles: the charge stream is not staged
-            launch_tiled<S, 8, 4, S == S_TSC ? 5 : 4, true>(c, a, tiles);
+            rc = launch_tiled<S, 8, 4, S == S_TSC ? 5 : 4, true>(c, a, tiles);
         else
-            launch_tiled<S, 8, 4, S == S_TSC ? 5 : 4, false>(c, a, tiles);
+            rc = launch_tiled<S, 8, 4, S == S_TSC ? 5 : 4, false>(c, a, tiles);
         prof_end(c);
+        if (rc != PIC_OK) return rc;
         return check_launch(c, "deposit_tiled");
     }
     int sms = 148;

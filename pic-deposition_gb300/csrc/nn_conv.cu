@@ -481,16 +481,10 @@ __global__ void reduce_wgrad_kernel(const float* __restrict__ partials, int grid
         db[co] = s;
 }
 
-template <typename K>
-int set_smem(K kernel, int bytes) {
-    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    return e == cudaSuccess ? PIC_OK : picgb::cuda_fail(e, "cudaFuncSetAttribute");
-}
-
 template <int CIN, int COUT, int EPI>
 int launch_conv_t(const ConvLaunch& a, cudaStream_t s) {
     using L = ConvSmem<CIN, COUT>;
-    static int attr = set_smem(conv3x3_kernel<CIN, COUT, EPI>, L::BYTES);
+    const int attr = picgb::opt_in_dynamic_smem((const void*)conv3x3_kernel<CIN, COUT, EPI>, L::BYTES);
     if (attr != PIC_OK) return attr;
     const dim3 grid(a.W / 128, (a.H + a.rows_per_cta - 1) / a.rows_per_cta, a.batch);
     conv3x3_kernel<CIN, COUT, EPI><<<grid, THREADS, L::BYTES, s>>>(a);
@@ -501,7 +495,7 @@ int launch_conv_t(const ConvLaunch& a, cudaStream_t s) {
 template <int CIN, int COUT>
 int launch_wgrad_t(const WgradLaunch& a, int grid, cudaStream_t s) {
     using L = WgSmem<CIN, COUT>;
-    static int attr = set_smem(wgrad_kernel<CIN, COUT>, L::BYTES);
+    const int attr = picgb::opt_in_dynamic_smem((const void*)wgrad_kernel<CIN, COUT>, L::BYTES);
     if (attr != PIC_OK) return attr;
     wgrad_kernel<CIN, COUT><<<grid, THREADS, L::BYTES, s>>>(a);
     const cudaError_t e = cudaGetLastError();

@@ -153,6 +153,9 @@ int cuda_fail(cudaError_t e, const char* what);
 int check_device_status(pic_ctx* ctx);
 // Launch-configuration error check after a kernel launch.
 int check_launch(pic_ctx* ctx, const char* what);
+// Raises `kernel`'s dynamic shared-memory limit on the current device to at least
+// `bytes` (the attribute is per device; recorded per kernel and device, thread-safe).
+int opt_in_dynamic_smem(const void* kernel, size_t bytes);
 
 void* dalloc(size_t bytes, int* rc);
 void dfree(void* p);

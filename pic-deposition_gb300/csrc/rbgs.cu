@@ -362,13 +362,8 @@ static int rbgs_solve_persistent(pic_ctx* c, const RbArgs& a, double tol, int ma
     const int ew = tw + 2 * PS_HALO, eh = th + 2 * PS_HALO;
     const size_t smem = (size_t)2 * ew * eh * sizeof(double);
     if (blocks > PS_MAX_BLOCKS || smem > 200 * 1024) return PIC_ERR_UNSUPPORTED;
-    static size_t smem_set = 0;
-    if (smem > 48 * 1024 && smem > smem_set) {
-        if (cudaFuncSetAttribute(rbgs_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-            return PIC_ERR_UNSUPPORTED;
-        smem_set = smem;
-    }
+    if (smem > 48 * 1024 && opt_in_dynamic_smem((const void*)rbgs_persistent, smem) != PIC_OK)
+        return PIC_ERR_UNSUPPORTED;
     int per_sm = 0, sms = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rbgs_persistent, PS_THREADS, smem);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
