@@ -8,8 +8,9 @@ cell-sorted once before timing.
 
 One step = one CIC charge deposition of all particles into an FP64 rho grid
 (clear + tiled fixed-point deposit + conversion), particles resident in HBM.
-The particle stream (1.07 GB) is far larger than L2 (129 MB), so no L2 flush is
-needed between steps.
+The particle stream (0.81 GB: cell, xr, yr, as every particle has the same charge;
+1.07 GB with per-particle charges) is far larger than L2 (129 MB), so no L2 flush
+is needed between steps.
 
   value   particles/s over the timed steps (CUDA events on the library stream),
           summed over ranks (replicas; one GPU each), max time over ranks.
@@ -19,7 +20,9 @@ needed between steps.
           when every particle has the same charge, as here -- the charge stream
           is not read -- else 16 B; + 8 B per cell) / its mean CUDA-event
           duration, against the measured HBM copy bandwidth in MEASURED_PEAKS.json.
-  cpu_baseline  the reference's FP64 CPU deposit on the host cores (rank 0).
+  cpu_baseline  the reference's FP64 CPU deposit on the host cores (rank 0);
+          its "detail" times every scheme at 1 and at all host threads, and the
+          reference's cell sort where it is built, on a 4 M-particle sample.
 
 --impl reference times the reference's own CPU path (oracle/_ref when it loads
 on this machine, else the oracle's C restatement of it) on the same workload,
@@ -266,6 +269,50 @@ def cpu_deposit_timer(threads: int):
     return run, kind
 
 
+def cpu_detail(ps, threads_all: int, sample: int = 4_000_000):
+    """The reference's CPU path per scheme and thread count, and its cell sort, each on
+    the first `sample` particles of the cell-sorted workload (a bounded sample).
+
+    FP64 deposit at 1 thread and at all host threads per scheme; TSC on one thread
+    only (the reference's privatised TSC writes past its per-thread grid, so its
+    parallel form is not timed). The sort (sortParticlesByCell: std::sort of indices
+    by cell, then a gather of the six arrays) is timed only where the compiled
+    reference loads, on a shuffled copy of the sample."""
+    m = min(sample, len(ps["x"]))
+    sl = {k: np.ascontiguousarray(v[:m]) for k, v in ps.items()}
+    timers = {th: cpu_deposit_timer(th) for th in sorted({1, threads_all})}
+    out = {"unit": "particles/s", "sample_particles": m, "kind": timers[1][1], "threads_all": threads_all,
+           "schemes": {}}
+    for name, code in SCHEMES.items():
+        row = {}
+        for th in ((1,) if name == "TSC" else sorted({1, threads_all})):
+            run = timers[th][0]
+            run(sl, code)  # warm-up
+            row[f"threads_{th}"] = m / min(run(sl, code) for _ in range(3))
+        out["schemes"][name] = row
+    import oracle
+
+    ref = None
+    if oracle.Ref.available():
+        try:
+            ref = oracle.Ref()
+        except OSError:
+            ref = None
+    if ref is None:
+        out["sort"] = {"unavailable": "the reference library is not built on this host (the port's sort "
+                                      "restates this project's stable radix sort, not the reference's)"}
+    else:
+        perm = np.random.default_rng(1).permutation(m)
+        sh = {k: np.ascontiguousarray(v[perm]) for k, v in sl.items()}
+        ref.sort(NX, NY, float(NX), float(NY), sh)
+        t0 = time.perf_counter()
+        ref.sort(NX, NY, float(NX), float(NY), sh)
+        t = time.perf_counter() - t0
+        out["sort"] = {"particles_per_s": m / t, "order": "random", "kind": "reference", "threads": 1,
+                       "includes": "copies of the six input arrays"}
+    return out
+
+
 def sorted_order(p):
     key = np.floor(p["y"]).astype(np.int64) * NX + np.floor(p["x"]).astype(np.int64)
     return np.argsort(key, kind="stable")
@@ -464,6 +511,10 @@ def run_gpu(args, d: Dist):
         cpu = {"value": n * reps / t_cpu, "unit": "particles/s", "cores": threads, "kind": kind,
                "sample": f"full workload ({n} cell-sorted particles), FP64 CIC deposit x{reps}, "
                          f"privatised OpenMP form of src/deposition/deposition_parallel.cpp"}
+        try:  # per scheme and thread count, and the sort; a failure here leaves the line intact
+            cpu["detail"] = cpu_detail(ps, threads)
+        except Exception as e:  # noqa: BLE001
+            cpu["detail"] = {"error": f"{type(e).__name__}: {e}"}
     for a in list(pin.values()) + [rho_host]:
         a.free()
     ctx.close()
