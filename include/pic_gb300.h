@@ -362,7 +362,9 @@ typedef struct pic_ens_run_info {
 int pic_ens_create(const pic_ens_member* runs, int nruns, const pic_ens_config* cfg, int device, pic_ens** out);
 int pic_ens_destroy(pic_ens* ens);
 /* Advances every run `steps` steps; field_energy and kinetic_energy (steps x nruns,
- * may be NULL) get each run's 0.5*sum(E^2)*dV after the solve and 0.5*m*sum(v^2). */
+ * may be NULL) get each run's 0.5*sum(E^2)*dV after the solve and 0.5*m*sum(v^2).
+ * PIC_ERR_TIMEOUT: a grid-wide barrier of the step kernel gave up (about one second);
+ * that step is incomplete, the error stays set, and the ensemble is to be destroyed. */
 int pic_ens_run(pic_ens* ens, int steps, double* field_energy, double* kinetic_energy);
 int pic_ens_num_runs(pic_ens* ens, int* n);
 int pic_ens_info(pic_ens* ens, int run, pic_ens_run_info* info);
