@@ -490,7 +490,8 @@ int orc_gs_ref(const orc_domain* d, const double* rho, int max_iters, double tol
 static double* rbgs_rhs(const orc_domain* d, const double* rho) {
     const size_t g = (size_t)d->Nx * d->Ny;
     const double scale = dom_dx(d) * dom_dy(d);
-    double* b = (double*)malloc(g * sizeof(double));
+    double* b = (double*)calloc(g ? g : 1, sizeof(double));
+    if (!b) return NULL;
     double s = 0.0;
     for (size_t i = 0; i < g; ++i) {
         b[i] = rho[i] * scale;
@@ -533,6 +534,7 @@ int orc_rbgs(const orc_domain* d, const double* rho, double* phi, double tol, in
     const double denom = 2.0 * (1.0 / dx2 + 1.0 / dy2);
     const double inv_denom = 1.0 / denom;
     double* b = rbgs_rhs(d, rho);
+    if (!b) return -2;
     if (check_every < 1) check_every = 1;
     double res = orc_rbgs_residual(d, b, phi);
     int it = 0;
