@@ -201,11 +201,8 @@ __device__ __forceinline__ void load_quad4(const StepArgs& a, size_t p0, bool ok
 
 // The step's particle work in one launch (see the file header).
 __global__ void __launch_bounds__(ENS_THREADS, 4) ens_step_kernel(StepArgs a) {
-    __shared__ uint32_t pbase[MAX_RUNS], cbase[MAX_RUNS];
-    for (int i = threadIdx.x; i < a.nruns; i += ENS_THREADS) {
-        pbase[i] = a.runs[i].pbase;
-        cbase[i] = a.runs[i].cell_base;
-    }
+    __shared__ uint32_t cbase[MAX_RUNS];
+    for (int i = threadIdx.x; i < a.nruns; i += ENS_THREADS) cbase[i] = a.runs[i].cell_base;
     __syncthreads();
     const size_t nthreads = (size_t)gridDim.x * ENS_THREADS;
     const size_t tid = (size_t)blockIdx.x * ENS_THREADS + threadIdx.x;
