@@ -137,17 +137,24 @@ typedef struct pic_gen_config {
     unsigned seed;
 } pic_gen_config;
 int pic_gpu_generate(pic_ctx* ctx, const pic_gen_config* cfg);
-/* Downloads particles back to FP64 SoA (positions rebuilt as (ix+xr)*dx). Any pointer may be NULL. */
+/* Downloads particles back to FP64 SoA (positions rebuilt as (ix+xr)*dx). Any pointer may be NULL.
+ * The reference keeps its particles in host memory (pic::ParticlesSoA, src/pic/particles.hpp:45-83);
+ * this returns the resident ones there. */
 int pic_gpu_download_particles(pic_ctx* ctx, double* x, double* y, double* vx, double* vy, double* q, double* m);
-/* Raw device layout, for bit-exact parity checks: any pointer may be NULL. */
+/* Raw device layout, for bit-exact parity checks: any pointer may be NULL (no counterpart
+ * in the reference). */
 int pic_gpu_download_device_layout(pic_ctx* ctx, uint32_t* cell, float* xr, float* yr, float* vx, float* vy,
                                    float* q);
+/* ParticlesSoA::size (src/pic/particles.hpp:45-83) of the resident set. */
 int pic_gpu_num_particles(pic_ctx* ctx, size_t* n_out);
 /* 1 when the resident particles are in cell order with valid per-cell offsets
- * (after pic_gpu_sort, or after an upload whose keys were already non-decreasing). */
+ * (after pic_gpu_sort, or after an upload whose keys were already non-decreasing).
+ * No counterpart: the reference sorts a copy on every sorted deposit
+ * (src/deposition/deposition.cpp:181-200). */
 int pic_gpu_is_sorted(pic_ctx* ctx, int* sorted_out);
 /* The stored charge q/max|q| shared by every resident particle (+-1), or 0 when
- * the charges differ. With one charge the kernels do not read the charge stream. */
+ * the charges differ. With one charge the kernels do not read the charge stream.
+ * No counterpart in the reference. */
 int pic_gpu_charge_uniform(pic_ctx* ctx, float* qn_out);
 
 /* ---- cell sort: replaces pic::sortParticlesByCell(ParticlesSoA&, const Domain&)
@@ -207,7 +214,8 @@ int pic_gpu_poisson_fft(pic_ctx* ctx);
 int pic_gpu_poisson_rbgs(pic_ctx* ctx, double tol, int max_iters, int warm_start, int check_every, int* iters_out,
                          double* resid_out);
 
-/* Arithmetic of the red-black Gauss-Seidel sweeps (this context, all later solves):
+/* Arithmetic of the red-black Gauss-Seidel sweeps (this context, all later solves; no
+ * counterpart: the reference's PoissonSolverGS, src/pic/poisson_gs.cpp:11-61, is FP64 only):
  * 0 (default) FP64 sweeps; 1 FP32 sweeps on a correction equation, refined in FP64
  * (r = b - A phi in FP64, A e = r relaxed in FP32, phi += e, until the FP64
  * relative residual meets tol). Both stop on the same FP64 test; mode 1 needs a
