@@ -49,6 +49,18 @@ def test_parallel_deposit_vs_reference(port, ref, scheme):
     assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
 
 
+def test_parallel_tsc_of_the_port(port, ref):
+    # the reference's privatised TSC is not used (it writes past its per-thread grid);
+    # the port's parallel TSC equals the serial one and the reference's serial TSC
+    # up to the FP64 summation order
+    p = port.init_particles(0, 32, 32, 1.0, 1.0, 20000, p0=1.0, seed=5)
+    a = port.deposit_ref(32, 32, 1.0, 1.0, TSC, p, threads=4)
+    b = port.deposit_ref(32, 32, 1.0, 1.0, TSC, p, threads=1)
+    c = ref.deposit(32, 32, 1.0, 1.0, TSC, p, threads=1)
+    assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
+    assert np.max(np.abs(a - c)) <= 1e-12 * np.max(np.abs(c))
+
+
 def test_sort_keys_and_cells_vs_reference(port, ref):
     p = port.init_particles(0, 20, 12, 2.0, 1.0, 5000, p0=1.0, seed=11)
     keys, perm, offs = port.stable_cell_sort(20, 12, 2.0, 1.0, p["x"], p["y"])
