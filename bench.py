@@ -234,12 +234,16 @@ def run_deposit_only(args, d: Dist):
     n = len(p["x"])
     with pg.Context(NX, NY, float(NX), float(NY), n) as ctx:
         ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
-        ctx.sort()
+        if args.order == "sorted":
+            ctx.sort()
+        else:  # the generation order, random with respect to cells
+            ctx.set_order(pg.ORDER_UNSORTED)
         ctx.profile(True)
         for _ in range(args.warmup + args.steps):
             ctx.deposit(SCHEMES[args.scheme], ESK_DT, download=False)
         ms, cnt = ctx.profile_read("deposit")
-    print(json.dumps({"deposit_only": args.scheme, "particles": n, "launches": cnt, "mean_kernel_ms": ms / cnt}))
+    print(json.dumps({"deposit_only": args.scheme, "order": args.order, "particles": n, "launches": cnt,
+                      "mean_kernel_ms": ms / cnt}))
 
 
 def cpu_deposit_timer(threads: int):
@@ -709,6 +713,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ppc", type=int, default=PPC, help="particles per cell (64 = the benchmark workload)")
     ap.add_argument("--deposit-only", action="store_true", help="reduced run for profilers")
+    ap.add_argument("--order", default="sorted", choices=["sorted", "random"],
+                    help="--deposit-only: cell-sorted particles or the generation order")
     ap.add_argument("--gs-only", action="store_true", help="only the Gauss-Seidel warm-start study")
     ap.add_argument("--no-gs", action="store_true", help="skip the Gauss-Seidel warm-start study")
     ap.add_argument("--c3-only", action="store_true", help="only the 2048^2 two-stream time step")

@@ -85,6 +85,8 @@ class Port:
         L.orc_field_energy.restype = C.c_double
         L.orc_to_device.argtypes = [D, C.c_size_t, _dp, _dp, _u32p, _fp, _fp]
         L.orc_normalize_charge.argtypes = [C.c_size_t, _dp, _fp, C.POINTER(C.c_float)]
+        L.orc_charge_uniform.argtypes = [C.c_size_t, _fp]
+        L.orc_charge_uniform.restype = C.c_int
         L.orc_deposit_fixed.argtypes = [D, C.c_int, C.c_size_t, _u32p, _fp, _fp, _fp, _fp, _fp, C.c_float, C.c_double,
                                         _i64p, C.POINTER(C.c_double)]
         L.orc_fixed_to_rho.argtypes = [C.c_size_t, _i64p, C.c_double, C.c_double, _dp]
@@ -255,6 +257,18 @@ class Port:
         mq = C.c_float(0)
         self.lib.orc_normalize_charge(len(q), q, qn, C.byref(mq))
         return qn, mq.value
+
+    def charge_uniform(self, qn) -> bool:
+        """True when every stored charge equals the first, nonzero and finite (the device's upload test)."""
+        qn = _c(qn, np.float32)
+        return bool(self.lib.orc_charge_uniform(len(qn), qn))
+
+    def fixed_total(self, scheme, qn) -> int:
+        """The exact int64 total of a deposit's grid: every particle deposits rint(qn * 2^24)
+        units, or 2^30 units in the exact integer TSC form (one charge for all particles)."""
+        if scheme == TSC and self.charge_uniform(qn):
+            return len(qn) << 30
+        return int(np.sum(np.rint(np.asarray(qn, np.float64) * 2 ** 24)))
 
     def deposit_fixed(self, nx, ny, lx, ly, scheme, cell, xr, yr, qn, maxq, vx32=None, vy32=None, dt=0.0):
         n = len(cell)

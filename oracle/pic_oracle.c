@@ -615,6 +615,8 @@ double orc_charge_error(double integrated_rho, double total_charge, double abs_c
 /* particle's own cell (frame offset 0, weight >= 1/64), otherwise the node   */
 /* of largest weight (first maximum of X and of Y). Sums are int64.           */
 /* unit = ((double)maxq * inv_vol) * 2^-24; rho = acc * unit + background.   */
+/* TSC with one charge for every particle uses exact integer weights        */
+/* instead (tsc_int_frame below; unit 2^-30 of the particle's charge).      */
 /* ======================================================================= */
 void orc_to_device(const orc_domain* d, size_t n, const double* x, const double* y, uint32_t* cell, float* xr,
                    float* yr) {
@@ -763,6 +765,42 @@ static int first_max(const float* X, int n) {
     return m;
 }
 
+/* ----------------------------------------------------------------------- */
+/* One charge for every particle (every stored qn bitwise equal, nonzero and */
+/* finite: the device's upload test), TSC: exact integer weights. Per axis,  */
+/* with t = r (r < 0.5) or r - 1 (r >= 0.5) as in tscWeights (ngp.cpp:28-34) */
+/* written relative to the cell,                                            */
+/*   WL = rint(2^14 (0.5 - t)^2) = rint(2^15 * 0.5 (0.5 - t)^2)             */
+/*   WR = rint(2^14 (0.5 + t)^2)                                            */
+/* each one FP32 fma (dl * (dl * 2^14) + 1.5*2^23: the product is exact and */
+/* the sum rounds once, to the nearest even integer), WC = 2^15 - WL - WR.  */
+/* The frame value of node (i, j) is WX[i] * WY[j], an exact integer; a     */
+/* particle deposits exactly 2^30 units and the charge sign sits in the     */
+/* unit: unit = ((double)maxq * inv_vol) * (qn * 2^-30).                    */
+/* ----------------------------------------------------------------------- */
+#define TSCI_ONE 32768
+static void tsc_int_frame(float r, int64_t W[4]) {
+    const int s = r >= 0.5f;
+    const float t = s ? r - 1.0f : r;
+    const float dl = 0.5f - t, dr = 0.5f + t;
+    const float fl = fmaf(dl, dl * 16384.0f, 12582912.0f);
+    const float fr = fmaf(dr, dr * 16384.0f, 12582912.0f);
+    const int64_t wl = (int64_t)(fl - 12582912.0f), wr = (int64_t)(fr - 12582912.0f);
+    const int64_t wc = TSCI_ONE - wl - wr;
+    W[0] = s ? 0 : wl;
+    W[1] = s ? wl : wc;
+    W[2] = s ? wc : wr;
+    W[3] = s ? wr : 0;
+}
+
+/* Nonzero when every qn equals the first, which is nonzero and finite. */
+int orc_charge_uniform(size_t n, const float* qn) {
+    if (n == 0 || !(qn[0] != 0.0f) || !isfinite(qn[0])) return 0;
+    for (size_t p = 1; p < n; ++p)
+        if (!(qn[p] == qn[0])) return 0;
+    return 1;
+}
+
 int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t* cell, const float* xr,
                       const float* yr, const float* vx, const float* vy, const float* qn, float maxq, double dt,
                       int64_t* acc, double* unit_out) {
@@ -770,6 +808,21 @@ int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t*
     const size_t g = (size_t)Nx * Ny;
     memset(acc, 0, g * sizeof(int64_t));
     const double inv_vol = 1.0 / (dom_dx(d) * dom_dy(d));
+    if (scheme == ORC_TSC && orc_charge_uniform(n, qn)) {
+        if (unit_out) *unit_out = ((double)maxq * inv_vol) * ((double)qn[0] * 0x1p-30);
+        for (size_t p = 0; p < n; ++p) {
+            const int ix = (int)(cell[p] % (uint32_t)Nx);
+            const int iy = (int)(cell[p] / (uint32_t)Nx);
+            int64_t X[4], Y[4];
+            tsc_int_frame(xr[p], X);
+            tsc_int_frame(yr[p], Y);
+            for (int j = 0; j < 4; ++j) {
+                const size_t row = (size_t)wrap_index(iy - 1 + j, Ny) * Nx;
+                for (int i = 0; i < 4; ++i) acc[row + wrap_index(ix - 1 + i, Nx)] += X[i] * Y[j];
+            }
+        }
+        return 0;
+    }
     if (unit_out) *unit_out = ((double)maxq * inv_vol) * 5.9604644775390625e-08;
     const float dtf = (float)dt;
     const float dtdx = (float)(dt / dom_dx(d));

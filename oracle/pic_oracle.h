@@ -75,6 +75,7 @@ double orc_charge_error(double integrated_rho, double total_charge, double abs_c
 void orc_to_device(const orc_domain* d, size_t n, const double* x, const double* y, uint32_t* cell, float* xr,
                    float* yr);
 void orc_normalize_charge(size_t n, const double* q, float* qn, float* maxq_out);
+int orc_charge_uniform(size_t n, const float* qn);
 int orc_deposit_fixed(const orc_domain* d, int scheme, size_t n, const uint32_t* cell, const float* xr,
                       const float* yr, const float* vx, const float* vy, const float* qn, float maxq, double dt,
                       int64_t* acc, double* unit_out);

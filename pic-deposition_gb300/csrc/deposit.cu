@@ -11,14 +11,17 @@
 //    (TSC: the particle's own cell node, weight >= 1/64; NGP/CIC/ESK: the node
 //    of largest weight), so every particle deposits exactly A units and
 //    total charge is exact. Sums are int64, so the result does not depend on
-//    summation order: the tiled, atomic and oracle paths agree bit for bit.
-//  * Sorted path (deposit_tiled). One CTA per tile of tile_w x tile_h cells;
-//    the particles of one row of the tile are one contiguous run of the
-//    cell-sorted stream, staged into shared memory with cp.async; each lane
-//    sums 8 consecutive particles per stage in registers while they share a
-//    cell and adds the run totals to the tile's accumulators in shared memory
-//    (split into two native 32-bit atomics); at the end the tile is flushed to
-//    the global int64 grid once. Details at the kernel.
+//    summation order: the sorted, any-order, atomic and oracle paths agree bit
+//    for bit. TSC with one charge for every particle uses exact integer
+//    weights instead (2^30 units per particle, see tsci_weights).
+//  * Sorted path (deposit_cells). One CTA per tile of tile_w x tile_h cells;
+//    one lane per cell of a 32-cell unit of a tile row walks the cell's
+//    contiguous range of the cell-sorted stream (staged into shared memory with
+//    cp.async), sums its particles' stencil values in registers and adds the
+//    cell's totals to the tile's accumulators in shared memory once (split
+//    into two native 32-bit atomics); at the end the tile is flushed to the
+//    global int64 grid once. A freshly sorted stream needs no cell keys: the
+//    offsets name every particle's cell. Details at the kernel.
 //  * Any-order path (deposit_runs): a warp handles 128 consecutive particles
 //    at a time, lane l taking particles 4l..4l+3 (one 128-bit streaming load
 //    per field, the next step's loads issued first); a lane sums its
@@ -462,6 +465,8 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_runs(DepArgs a) {
     }
 }
 
+__device__ __forceinline__ void tsci_particle_to_global(const DepArgs& a, uint32_t key, float rx, float ry);
+
 template <int S>
 __global__ void __launch_bounds__(DEP_THREADS) deposit_atomic(DepArgs a) {
     constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
@@ -471,6 +476,12 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_atomic(DepArgs a) {
         if (key >= G) {
             set_dev_error(a.st, DEV_BAD_CELL, (unsigned)p);
             continue;
+        }
+        if constexpr (S == S_TSC) {
+            if (a.qc != 0.0f) {  // one charge for all particles: exact integer weights
+                tsci_particle_to_global(a, key, __ldcs(a.xr + p), __ldcs(a.yr + p));
+                continue;
+            }
         }
         const int iy = (int)(key / (uint32_t)a.Nx), ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
         int val[V];
@@ -537,6 +548,95 @@ __device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
+
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// TSC with one charge for every particle: exact integer weights.
+// Per axis, with t = r (r < 0.5) or r - 1 (r >= 0.5) as above, the outer
+// weights are WL = rint(2^14 (0.5 - t)^2) and WR = rint(2^14 (0.5 + t)^2),
+// each one FP32 fma (d * (d * 2^14) + 1.5*2^23: the product is exact, the sum
+// rounds once to the nearest even integer), and WC = 2^15 - WL - WR, so an
+// axis' three weights sum to 2^15 exactly (tscWeights, ngp.cpp:28-34, at
+// 2^-15 resolution: rho within about 2.3e-6 relative L2 of the FP64 deposit at
+// 64 particles per cell). A frame value WX[i] * WY[j] is an exact integer
+// product (no rounding, no remainder step) and a particle deposits exactly
+// 2^30 units; the charge and its sign sit in the unit, qn * max|q| * inv_vol *
+// 2^-30. Bounds: the 12 frame entries outside the central 2x2 are at most
+// 2^12 * 24576 < 2^26.6 per particle (32-bit sums for runs of up to 32
+// particles); the central 4 at most 24576^2 = 0.5625 * 2^30 (64-bit sums).
+// ---------------------------------------------------------------------------
+constexpr uint32_t TSCI_ONE = 1u << 15;
+
+__device__ __forceinline__ void tsci_weights(float rx, float ry, uint32_t (&X)[4], uint32_t (&Y)[4]) {
+    const bool sx = rx >= 0.5f, sy = ry >= 0.5f;
+    float mx, my;
+    f2_unpack(f2_add(f2_pack(rx, ry), f2_pack(-1.0f, -1.0f)), mx, my);
+    const f32x2 t = f2_pack(sx ? mx : rx, sy ? my : ry);
+    const f32x2 half = f2_pack(0.5f, 0.5f);
+    const f32x2 dl = f2_sub(half, t), dr = f2_add(half, t);
+    const f32x2 s14 = f2_pack(16384.0f, 16384.0f), mag = f2_pack(TSC_MAGIC, TSC_MAGIC);
+    const f32x2 wl = f2_fma(dl, f2_mul(dl, s14), mag), wr = f2_fma(dr, f2_mul(dr, s14), mag);
+    float lx, ly, rxw, ryw;
+    f2_unpack(wl, lx, ly);
+    f2_unpack(wr, rxw, ryw);
+    const uint32_t WLx = __float_as_uint(lx) - TSC_MAGIC_BITS, WLy = __float_as_uint(ly) - TSC_MAGIC_BITS;
+    const uint32_t WRx = __float_as_uint(rxw) - TSC_MAGIC_BITS, WRy = __float_as_uint(ryw) - TSC_MAGIC_BITS;
+    const uint32_t WCx = TSCI_ONE - WLx - WRx, WCy = TSCI_ONE - WLy - WRy;
+    X[0] = sx ? 0u : WLx;
+    X[1] = sx ? WLx : WCx;
+    X[2] = sx ? WCx : WRx;
+    X[3] = sx ? WRx : 0u;
+    Y[0] = sy ? 0u : WLy;
+    Y[1] = sy ? WLy : WCy;
+    Y[2] = sy ? WCy : WRy;
+    Y[3] = sy ? WRy : 0u;
+}
+
+// c + a * b in 64 bits, one multiply-add (a widening multiply followed by a
+// separate 64-bit add takes three instructions)
+__device__ __forceinline__ unsigned long long mad_wide(uint32_t a, uint32_t b, unsigned long long c) {
+    unsigned long long d;
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+    return d;
+}
+
+// Frame entry q (row-major j*4+i) -> slot among the 12 outer or the 4 central entries.
+__host__ __device__ constexpr int tsci_outer_slot(int q) { return q < 5 ? q : q < 7 ? 4 : q < 8 ? 5 : q < 9 ? 6 : q < 11 ? 7 : q - 4; }
+__host__ __device__ constexpr int tsci_central_slot(int q) { return q == 5 ? 0 : q == 6 ? 1 : q == 9 ? 2 : 3; }
+
+// The frame sums of a run of particles of one cell (exact).
+struct TscIntSums {
+    uint32_t o[12];
+    unsigned long long c[4];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) o[k] = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) c[k] = 0;
+    }
+    __device__ __forceinline__ void add(float rx, float ry) {
+        uint32_t X[4], Y[4];
+        tsci_weights(rx, ry, X, Y);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int q = j * 4 + i;
+                if (tsc_central(q))
+                    c[tsci_central_slot(q)] = mad_wide(X[i], Y[j], c[tsci_central_slot(q)]);
+                else
+                    o[tsci_outer_slot(q)] += X[i] * Y[j];
+            }
+    }
+    __device__ __forceinline__ long long get(int q) const {
+        return tsc_central(q) ? (long long)c[tsci_central_slot(q)] : (long long)o[tsci_outer_slot(q)];
+    }
+};
 
 // Frame values: central entries exact, the others biased by TSC_MAGIC_BITS.
 // Both axes' weights are computed as pairs (x, y) and the products of a frame
@@ -607,15 +707,36 @@ __device__ __forceinline__ int tsc_true(int q, uint32_t acc, uint32_t cnt) {
     return tsc_central(q) ? (int)acc : (int)(acc - cnt * TSC_MAGIC_BITS);
 }
 
+// Adds one particle's exact integer TSC values (one charge for all particles)
+// straight to the global grid.
+__device__ __forceinline__ void tsci_particle_to_global(const DepArgs& a, uint32_t key, float rx, float ry) {
+    const int iy = (int)(key / (uint32_t)a.Nx), ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
+    uint32_t X[4], Y[4];
+    tsci_weights(rx, ry, X, Y);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const size_t row = (size_t)wrap_i(iy - 1 + j, a.Ny) * a.Nx;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const unsigned long long v = (unsigned long long)X[i] * Y[j];
+            if (v != 0) atomicAdd(a.acc + row + wrap_i(ix - 1 + i, a.Nx), v);
+        }
+    }
+}
+
 // A particle outside the tile row whose slice of the stream holds it (the cell
 // ranges are those of an earlier sort and the particle has moved since): its
 // values go straight to the global int64 grid.
-template <int S>
+template <int S, bool QC>
 __device__ __forceinline__ void particle_to_global(const DepArgs& a, uint32_t key, float rx, float ry, float qn,
                                                 float vxx, float vyy, uint32_t p) {
     constexpr int NV = Frame<S>::NX * Frame<S>::NX;
     if (key >= (uint32_t)a.Nx * (uint32_t)a.Ny) {
         set_dev_error(a.st, DEV_BAD_CELL, p);
+        return;
+    }
+    if constexpr (S == S_TSC && QC) {
+        tsci_particle_to_global(a, key, rx, ry);
         return;
     }
     const int iy = (int)(key / (uint32_t)a.Nx), ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
@@ -634,38 +755,37 @@ __device__ __forceinline__ void particle_to_global(const DepArgs& a, uint32_t ke
     flush_global<S>(a, key, tv);
 }
 
-// Sorted path. One CTA of NW warps per tile of tile_w x tile_h cells. The
-// particles of one row of the tile are the contiguous slice
-// [offsets[c0], offsets[c0+tile_w]) of the cell-sorted stream; warp w walks
-// rows w, w+NW, ... and cuts each slice (from its 16-byte-aligned start) into
-// stages of 32*LPP consecutive particles.
-//  * Staging: a stage's fields are copied global -> shared with cp.async
-//    (16 bytes per lane and copy, each warp copy 512 contiguous bytes), two
-//    stage buffers per warp, the next stage in flight while this one is used.
-//    Quad Q (particles 4Q..4Q+3) of a field sits at slot Q ^ ((Q>>3)&(LPP/4-1)),
-//    which makes both the copies and the lanes' 128-bit reads conflict-free.
-//  * Lane chunks: lane l owns particles LPP*l .. LPP*l+LPP-1 of the stage and
-//    sums the values of the run of equal cells it is in, in 16 (TSC) or 4
-//    (CIC, NGP) registers; when its cell changes, the finished run moves to
-//    the lane's slots in shared memory (written out when a third run starts),
-//    and at the end of the chunk both runs are written out. No warp-wide
-//    scan; lanes are idle only at the ends of a slice. |value| <= 2^24 + 3 per
-//    particle and entry, so a run of LPP <= 16 particles fits in int32.
-//  * Tile accumulators: 64-bit shared atomics are not native (they compile to
-//    compare-and-swap loops), so a run total v is added as two native 32-bit
-//    shared atomics, v & (2^15-1) to an unsigned low word and v >> 15 to a
-//    signed high word; the node's total is hi * 2^15 + lo. A node receives at
-//    most one addition per run, and a run holds at least one particle of the
-//    tile, so both words stay exact while the tile holds fewer than 2^17
-//    particles (|v| < 2^29). Denser tiles add their runs straight to the
-//    global int64 grid.
-// At the end the tile is added to the global int64 grid once.
-// cell, xr, yr, q (not when uniform) (, vx, vy)
+// Adds a lane's run totals for cell `key` (64-bit values) straight to the global grid.
+template <int NX, int LO, int NV>
+__device__ __forceinline__ void flush_global_ll(const DepArgs& a, uint32_t key, const long long (&tv)[NV]) {
+    const int iy = (int)(key / (uint32_t)a.Nx), ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
+#pragma unroll
+    for (int j = 0; j < NX; ++j) {
+        const size_t row = (size_t)wrap_i(iy + LO + j, a.Ny) * a.Nx;
+#pragma unroll
+        for (int i = 0; i < NX; ++i) {
+            const long long v = tv[j * NX + i];
+            if (v != 0) atomicAdd(a.acc + row + wrap_i(ix + LO + i, a.Nx), (unsigned long long)v);
+        }
+    }
+}
+
+// Fields of a particle staged by the sorted kernel: cell, xr, yr, q (not when
+// one charge is shared), vx, vy (Esirkepov).
 template <int S, bool QC>
 struct StageFields {
     static constexpr int NF = (S == S_ESK ? 6 : 4) - (QC ? 1 : 0);
 };
 
+// Tile accumulators: 64-bit shared atomics are not native (they compile to
+// compare-and-swap loops), so a cell's total v is added as two native 32-bit
+// shared atomics, v & (2^15-1) to an unsigned low word and v >> 15 to a high
+// word; the node's total is hi * 2^15 + lo. A node receives at most 16
+// additions per cell (one per neighbouring cell), so the low words stay exact;
+// the high words stay exact while the tile holds fewer than 2^17 particles
+// (signed, |value| <= 2^24 + 3 per particle and node in the general form;
+// unsigned in the exact integer TSC form, at most 0.5625 * 2^30 per particle).
+// Denser tiles add their cells' totals straight to the global int64 grid.
 constexpr int TILE_SPLIT = 15;
 constexpr uint32_t TILE_SPLIT_MAX = 1u << 17;  // particles per tile for the split accumulators
 
@@ -675,256 +795,79 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
-template <int LPP>
-__device__ __forceinline__ int stage_slot(int Q) {
-    return Q ^ ((Q >> 3) & (LPP / 4 - 1));
+// Adds a run's exact integer TSC totals for cell `key` straight to the global
+// grid, without integer division (as flush_global_nd).
+__device__ __forceinline__ void tsci_flush_global_nd(const DepArgs& a, uint32_t key, float inv_nx, const TscIntSums& s) {
+    int iy, ix;
+    split_key(key, a.Nx, inv_nx, iy, ix);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const size_t row = (size_t)wrap_near(iy - 1 + j, a.Ny) * a.Nx;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const unsigned long long v = (unsigned long long)s.get(j * 4 + i);
+            if (v != 0) atomicAdd(a.acc + row + wrap_near(ix - 1 + i, a.Nx), v);
+        }
+    }
 }
 
-// Shared memory: [alignment pad][stage buffers: NW warps x 2 x NF fields x
-// LPP*128 bytes, 1024-byte aligned (measured 2-3 % faster than unaligned)]
-// [lanes' previous-run sums: NW x NV x 32 words, [entry][lane]][tile accumulators].
-template <int S, int LPP, int NW, bool QC>
-__host__ __device__ constexpr size_t tiled_stage_bytes() {
-    return (size_t)NW * 2 * StageFields<S, QC>::NF * (32 * LPP) * 4;
-}
-template <int S, int LPP, int NW, bool QC>
-__host__ __device__ constexpr size_t tiled_fixed_bytes() {
-    return 1024 + tiled_stage_bytes<S, LPP, NW, QC>() + (size_t)NW * 32 * 4 * Frame<S>::NX * Frame<S>::NX;
-}
-
-template <int S, int LPP, int NW, int MINB, bool QC>
-__global__ void __launch_bounds__(NW * 32, MINB) deposit_tiled(DepArgs a) {
-    constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
-    constexpr int NV = NX * NX;
-    constexpr int NF = StageFields<S, QC>::NF;
-    constexpr int FV = QC ? 3 : 4;  // stage field of vx (ESK)
-    constexpr int QL = LPP / 4;          // quads per lane per stage
-    constexpr int STAGE = 32 * LPP;      // particles per stage
-    constexpr int FB = STAGE * 4;        // bytes per field per stage buffer
-    static_assert(LPP % 4 == 0 && LPP <= 16, "a lane's run of LPP particles must fit in int32");
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ uint32_t s_count;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int SW = a.tile_w + 3;
-    const int tx = blockIdx.x % a.tiles_x, ty = blockIdx.x / a.tiles_x;
-    const int x0 = tx * a.tile_w, y0 = ty * a.tile_h;
-    const int tw = min(a.tile_w, a.Nx - x0), th = min(a.tile_h, a.Ny - y0);
-    const int nloc = (th + 3) * SW;
-    const uint32_t sraw = (uint32_t)__cvta_generic_to_shared(smem_raw);
-    unsigned char* sstage = smem_raw + ((1024u - (sraw & 1023u)) & 1023u);  // 1024-byte aligned
-    unsigned char* swarp = sstage + (size_t)warp * 2 * NF * FB;
-    const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(swarp);
-    uint32_t* prv = reinterpret_cast<uint32_t*>(sstage + tiled_stage_bytes<S, LPP, NW, QC>()) + warp * 32 * NV + lane;
-    uint32_t* slo = reinterpret_cast<uint32_t*>(smem_raw + tiled_fixed_bytes<S, LPP, NW, QC>());
-    int* shi = reinterpret_cast<int*>(slo + nloc);
-    if (threadIdx.x == 0) s_count = 0;
-    for (int i = threadIdx.x; i < nloc; i += NW * 32) {
-        slo[i] = 0;
-        shi[i] = 0;
-    }
-    __syncthreads();
-    if (threadIdx.x < th) {
-        const uint32_t c0 = (uint32_t)(y0 + threadIdx.x) * (uint32_t)a.Nx + (uint32_t)x0;
-        atomicAdd(&s_count, a.offsets[c0 + tw] - a.offsets[c0]);
-    }
-    __syncthreads();
-    const bool dense = s_count >= TILE_SPLIT_MAX;
-
-    const void* fptr[NF];
-    fptr[0] = a.cell;
-    fptr[1] = a.xr;
-    fptr[2] = a.yr;
-    if constexpr (!QC) fptr[3] = a.q;
-    if constexpr (S == S_ESK) {
-        fptr[FV] = a.vx;
-        fptr[FV + 1] = a.vy;
-    }
-    // tile row r: first particle, end, aligned start, stages
-    struct Slice {
-        uint32_t pbeg, pend, base, nst;
-    };
-    auto slice = [&](int r) {
-        Slice sl;
-        const uint32_t c0 = (uint32_t)(y0 + r) * (uint32_t)a.Nx + (uint32_t)x0;
-        sl.pbeg = a.offsets[c0];
-        sl.pend = a.offsets[c0 + tw];
-        sl.base = sl.pbeg & ~3u;
-        sl.nst = sl.pend > sl.pbeg ? (sl.pend - sl.base + STAGE - 1) / STAGE : 0u;
-        return sl;
-    };
-    auto issue = [&](const Slice& sl, uint32_t t, int buf) {
-        const uint32_t dst = stage0 + (uint32_t)(buf * NF * FB);
-        const uint32_t sbase = sl.base + t * STAGE;
+// Any-order path for TSC with one charge for all particles (exact integer
+// weights): the warp step of deposit_runs with the run sums of TscIntSums. The
+// scan's segments stop at lanes 8, 16 and 24, so a run total covers at most 32
+// particles and the 12 outer entries stay below 32 * 2^26.6 < 2^32.
+__global__ void __launch_bounds__(DEP_THREADS, 4) deposit_runs_tsci(DepArgs a) {
+    const int lane = threadIdx.x & 31;
+    const size_t gw = (size_t)blockIdx.x * DEP_WARPS + (threadIdx.x >> 5);
+    const size_t stride = (size_t)gridDim.x * DEP_WARPS * 128;
+    const uint32_t G = (uint32_t)a.Nx * (uint32_t)a.Ny;
+    const float inv_nx = 1.0f / (float)a.Nx;
+    const unsigned upto = (lane == 31) ? FULL : ((2u << lane) - 1u);
+    size_t base = gw * 128;
+    Quad<S_TSC> cur, nxt;
+    load_quad<S_TSC>(a, (uint32_t)(base + 4u * lane), base + 4u * lane < a.n, cur);
+    for (; base < a.n; base += stride) {
+        const size_t nbase = base + stride;
+        if (nbase < a.n) load_quad<S_TSC>(a, (uint32_t)(nbase + 4u * lane), nbase + 4u * lane < a.n, nxt);
+        uint32_t ckey = NO_CELL;
+        TscIntSums s;
+        s.zero();
 #pragma unroll
-        for (int k = 0; k < QL; ++k) {
-            const int Q = k * 32 + lane;
-            const uint32_t p = sbase + 4u * (uint32_t)Q;
-            if (p < sl.pend) {
-#pragma unroll
-                for (int f = 0; f < NF; ++f)
-                    cp_async16(dst + (uint32_t)(f * FB + stage_slot<LPP>(Q) * 16),
-                               static_cast<const uint32_t*>(fptr[f]) + p);
-            }
-        }
-        cp_async_commit();
-    };
-
-    int r = warp;
-    Slice cs{0u, 0u, 0u, 0u};
-    while (r < th) {
-        cs = slice(r);
-        if (cs.nst) break;
-        r += NW;
-    }
-    if (r < th) issue(cs, 0u, 0);
-    uint32_t t = 0;
-    int buf = 0;
-    while (r < th) {
-        // the stage after this one: next stage of this row or first of the next non-empty row
-        int rn = r;
-        uint32_t tn = t + 1;
-        Slice ns = cs;
-        if (tn >= cs.nst) {
-            tn = 0;
-            ns.nst = 0;
-            for (rn = r + NW; rn < th; rn += NW) {
-                ns = slice(rn);
-                if (ns.nst) break;
-            }
-        }
-        if (rn < th) {
-            issue(ns, tn, buf ^ 1);
-        } else {
-            cp_async_commit();
-        }
-        cp_async_wait_1();
-        __syncwarp();
-
-        const int iy = y0 + r;
-        const uint32_t rowbase = (uint32_t)iy * (uint32_t)a.Nx;
-        const uint32_t c0 = rowbase + (uint32_t)x0;
-        const int lrow = r + 1 + LO;   // local row of frame row 0
-        const int lcol = 1 + LO - x0;  // local column of frame column 0 is ix + lcol
-        const unsigned char* sb = swarp + (size_t)buf * NF * FB;
-        // this lane's particles in this stage: [vbeg, vbeg + vlen) of the stream
-        const uint32_t cstart = cs.base + t * STAGE + (uint32_t)(LPP * lane);
-        const uint32_t vbeg = max(cstart, cs.pbeg), vend = min(cstart + LPP, cs.pend);
-        const uint32_t vlen = vend > vbeg ? vend - vbeg : 0u;
-        uint32_t ckey = NO_CELL, cnt = 0, pkey = NO_CELL, pcnt = 0;
-        uint32_t acc[NV];
-#pragma unroll
-        for (int q = 0; q < NV; ++q) acc[q] = 0;
-        // writes out a run: sums in registers (acc) or in the lane's shared slots (prv)
-        auto flush = [&](bool from_prv, uint32_t key, uint32_t n) {
-            if (dense) {
-                int tv[NV];
-#pragma unroll
-                for (int q = 0; q < NV; ++q) {
-                    const uint32_t v = from_prv ? prv[32 * q] : acc[q];
-                    if constexpr (S == S_TSC)
-                        tv[q] = tsc_true(q, v, n);
-                    else
-                        tv[q] = (int)v;
+        for (int k = 0; k < 4; ++k) {
+            const size_t p = base + 4u * lane + (size_t)k;
+            if (p < a.n) {
+                const uint32_t key = u4(cur.cell, k);
+                if (key >= G) {
+                    set_dev_error(a.st, DEV_BAD_CELL, (unsigned)p);
+                    continue;
                 }
-                flush_global<S>(a, key, tv);
-                return;
-            }
-            const int lx = (int)(key - rowbase) + lcol;
-#pragma unroll
-            for (int q = 0; q < NV; ++q) {
-                const uint32_t v = from_prv ? prv[32 * q] : acc[q];
-                int x;
-                if constexpr (S == S_TSC)
-                    x = tsc_true(q, v, n);
-                else
-                    x = (int)v;
-                if (x != 0) {
-                    const int i = (lrow + q / NX) * SW + lx + (q % NX);
-                    atomicAdd(slo + i, (uint32_t)x & ((1u << TILE_SPLIT) - 1u));
-                    atomicAdd(shi + i, x >> TILE_SPLIT);
+                if (key != ckey) {
+                    if (ckey != NO_CELL) tsci_flush_global_nd(a, ckey, inv_nx, s);
+                    ckey = key;
+                    s.zero();
                 }
+                s.add(f4(cur.xr, k), f4(cur.yr, k));
             }
-        };
+        }
+        const uint32_t kprev = __shfl_up_sync(FULL, ckey, 1);
+        const unsigned H = __ballot_sync(FULL, (lane & 7) == 0 || ckey != kprev);
+        const int segstart = 31 - __clz(H & upto);
 #pragma unroll
-        for (int h = 0; h < QL; ++h) {
-            const int Q = QL * lane + h;
-            const int off = stage_slot<LPP>(Q) * 16;
-            Quad<S> d;
-            d.cell = *reinterpret_cast<const uint4*>(sb + 0 * FB + off);
-            d.xr = *reinterpret_cast<const float4*>(sb + 1 * FB + off);
-            d.yr = *reinterpret_cast<const float4*>(sb + 2 * FB + off);
-            if constexpr (QC)
-                d.q = make_float4(a.qc, a.qc, a.qc, a.qc);
-            else
-                d.q = *reinterpret_cast<const float4*>(sb + 3 * FB + off);
-            if constexpr (S == S_ESK) {
-                d.vx = *reinterpret_cast<const float4*>(sb + FV * FB + off);
-                d.vy = *reinterpret_cast<const float4*>(sb + (FV + 1) * FB + off);
+        for (int d = 1; d < 8; d <<= 1) {
+            const bool take = lane - d >= segstart;
+#pragma unroll
+            for (int k = 0; k < 12; ++k) {
+                const uint32_t o = __shfl_up_sync(FULL, s.o[k], d);
+                if (take) s.o[k] += o;
             }
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const uint32_t p = cstart + (uint32_t)(4 * h + k);
-                if (p - vbeg < vlen) {
-                    const uint32_t key = u4(d.cell, k);
-                    if (key - c0 >= (uint32_t)tw) {  // left this tile row since the last sort
-                        float vxx = 0.0f, vyy = 0.0f;
-                        if constexpr (S == S_ESK) {
-                            vxx = f4(d.vx, k);
-                            vyy = f4(d.vy, k);
-                        }
-                        particle_to_global<S>(a, key, f4(d.xr, k), f4(d.yr, k), f4(d.q, k), vxx, vyy, p);
-                        continue;
-                    }
-                    if (key != ckey) {  // a new run: divergent only at cell boundaries
-                        if (ckey != NO_CELL) {
-                            if (pkey != NO_CELL) flush(true, pkey, pcnt);
-#pragma unroll
-                            for (int q = 0; q < NV; ++q) {
-                                prv[32 * q] = acc[q];
-                                acc[q] = 0;
-                            }
-                            pkey = ckey;
-                            pcnt = cnt;
-                            cnt = 0;
-                        }
-                        ckey = key;
-                    }
-                    if constexpr (S == S_TSC) {
-                        tsc_accumulate(f4(d.xr, k), f4(d.yr, k), f4(d.q, k), acc);
-                    } else {
-                        int iv[V];
-                        float vxx = 0.0f, vyy = 0.0f;
-                        if constexpr (S == S_ESK) {
-                            vxx = f4(d.vx, k);
-                            vyy = f4(d.vy, k);
-                        }
-                        if (!stencil_values<S>(a, f4(d.xr, k), f4(d.yr, k), f4(d.q, k), vxx, vyy,
-                                               (int)(key - rowbase), iy, p, iv))
-                            continue;  // deposited by the general trajectory path
-#pragma unroll
-                        for (int q = 0; q < NV; ++q) acc[q] += (uint32_t)iv[q];
-                    }
-                    ++cnt;
-                }
+                const unsigned long long o = __shfl_up_sync(FULL, s.c[k], d);
+                if (take) s.c[k] += o;
             }
         }
-        if (ckey != NO_CELL) flush(false, ckey, cnt);
-        if (pkey != NO_CELL) flush(true, pkey, pcnt);
-        __syncwarp();
-        r = rn;
-        t = tn;
-        cs = ns;
-        buf ^= 1;
-    }
-    __syncthreads();
-    if (dense) return;
-    for (int i = threadIdx.x; i < nloc; i += NW * 32) {
-        const long long v = (long long)shi[i] * (1ll << TILE_SPLIT) + (long long)slo[i];
-        if (v != 0) {
-            const int ly = i / SW, lx = i % SW;
-            const int gx = wrap_i(x0 - 1 + lx, a.Nx), gy = wrap_i(y0 - 1 + ly, a.Ny);
-            atomicAdd(a.acc + (size_t)gy * a.Nx + gx, (unsigned long long)v);
-        }
+        const bool tail = (lane == 31) || ((H >> (lane + 1)) & 1u);
+        if (tail && ckey != NO_CELL) tsci_flush_global_nd(a, ckey, inv_nx, s);
+        cur = nxt;
     }
 }
 
@@ -1000,9 +943,393 @@ __global__ void __launch_bounds__(DEP_THREADS, 4) deposit_runs_tsc(DepArgs a) {
     }
 }
 
-// One unit of the int64 grid (FP64).
-__global__ void fixed_unit(double inv_vol, const DevStats* st, double* unit_out) {
-    *unit_out = charge_unit(st, inv_vol);
+// ---------------------------------------------------------------------------
+// Sorted path, cell form (deposit_cells). One CTA of NW warps per tile of
+// tile_w x tile_h cells; the tile's rows are cut into units of up to 32
+// consecutive cells and warp w walks units w, w+NW, ... Lane l of a unit owns
+// one cell: the contiguous range [offsets[c], offsets[c+1]) of the cell-sorted
+// stream, which it walks in stages of LPP particles.
+//  * Staging: each stage's quads (4 particles, from the 16-byte boundary at or
+//    below the cell's first particle) are copied global -> shared with
+//    cp.async, 16 bytes per lane, field and quad, into [field][quad][lane]
+//    slots (the copies and the lanes' 128-bit reads are conflict-free); two
+//    stage buffers per warp, the next stage -- or the next unit's first -- in
+//    flight while this one is used. A unit takes as many stages as its fullest
+//    cell; lanes whose cell is done idle.
+//  * A lane's particles all belong to its cell, so there are no runs to detect
+//    and no cell keys to read: the offsets name every particle's cell (KEYS =
+//    false, a fresh sort). After particles have moved since the sort (KEYS =
+//    true) the keys are read, and a particle that left its cell goes straight
+//    to the global grid.
+//  * Sums: per stage in 32 bits (at most LPP particles), added to 64-bit cell
+//    totals at the end of each stage (CellRun); the exact integer TSC form
+//    keeps 9 of its 16 entries and 6 axis sums (see CellRun<S_TSC, true>).
+//  * Each lane writes its cell's totals out once: to the tile's split 32-bit
+//    shared accumulators (adjacent lanes hit different nodes: no same-address
+//    conflicts), or, in a tile of 2^17 particles or more, to the global grid.
+// At the end the tile is added to the global int64 grid once.
+// ---------------------------------------------------------------------------
+template <int S, bool QC>
+struct CellRun {
+    static constexpr int NV = Frame<S>::NX * Frame<S>::NX;
+    uint32_t v[NV];   // this stage's sums (TSC: outer entries biased, see tsc_accumulate)
+    long long T[NV];  // the cell's totals
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            v[q] = 0;
+            T[q] = 0;
+        }
+    }
+    __device__ __forceinline__ void end_quad() {}
+    __device__ __forceinline__ void finish() {}
+    // adds the sums of stage t (`cnt` particles) to the totals
+    __device__ __forceinline__ void end_stage(uint32_t cnt, uint32_t) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            if constexpr (S == S_TSC)
+                T[q] += tsc_true(q, v[q], cnt);
+            else
+                T[q] += (int)v[q];
+            v[q] = 0;
+        }
+    }
+    __device__ __forceinline__ void totals(uint32_t, long long (&A)[NV]) const {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) A[q] = T[q];
+    }
+};
+
+// TSC with one charge for all particles. Every particle's frame is X (x) Y
+// with sum_i X[i] = sum_j Y[j] = 2^15, so a cell's 4x4 sums A[j][i] have row
+// sums 2^15 * SY[j] and column sums 2^15 * SX[i] (SX, SY: the sums of each
+// axis' weights). The lane keeps the 9 entries A[j][i] with i, j in {0, 1, 3}
+// and the axis sums SX[0,1,3], SY[0,1,3]; row 2, column 2 and SX[2], SY[2]
+// follow exactly (integer identities) when the cell is written out. Per
+// particle: 9 32-bit multiply-adds and 6 adds. Bounds: the 8 entries other than
+// A[1][1] are at most 2^12 * 24576 < 2^26.6 per particle, summed in 32 bits for
+// 4 stages (at most 32 particles) and then added to 64-bit totals; A[1][1] <=
+// 24576^2 < 2^29.2 per particle is summed in 32 bits for a quad (4 particles);
+// the axis sums are 64-bit totals of 32-bit sums of 4 stages.
+template <>
+struct CellRun<S_TSC, true> {
+    static constexpr int NV = 16;
+    uint32_t e[8], c11;            // partial sums of the current stage / quad
+    unsigned long long E[8], C11;  // A00 A01 A03 A10 A13 A30 A31 A33, A11
+    uint32_t sx0, sx1, sx3, sy0, sy1, sy3;
+    unsigned long long SX0, SX1, SX3, SY0, SY1, SY3;
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            e[k] = 0;
+            E[k] = 0;
+        }
+        c11 = 0;
+        C11 = 0;
+        sx0 = sx1 = sx3 = sy0 = sy1 = sy3 = 0;
+        SX0 = SX1 = SX3 = SY0 = SY1 = SY3 = 0;
+    }
+    __device__ __forceinline__ void add(float rx, float ry) {
+        uint32_t X[4], Y[4];
+        tsci_weights(rx, ry, X, Y);
+        e[0] += X[0] * Y[0];
+        e[1] += X[1] * Y[0];
+        e[2] += X[3] * Y[0];
+        e[3] += X[0] * Y[1];
+        e[4] += X[3] * Y[1];
+        e[5] += X[0] * Y[3];
+        e[6] += X[1] * Y[3];
+        e[7] += X[3] * Y[3];
+        c11 += X[1] * Y[1];
+        sx0 += X[0];
+        sx1 += X[1];
+        sx3 += X[3];
+        sy0 += Y[0];
+        sy1 += Y[1];
+        sy3 += Y[3];
+    }
+    __device__ __forceinline__ void end_quad() {
+        C11 += c11;
+        c11 = 0;
+    }
+    // partial sums -> 64-bit totals (every 4 stages: at most 32 particles, 2^31.6)
+    __device__ __forceinline__ void fold() {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            E[k] += e[k];
+            e[k] = 0;
+        }
+        SX0 += sx0;
+        SX1 += sx1;
+        SX3 += sx3;
+        SY0 += sy0;
+        SY1 += sy1;
+        SY3 += sy3;
+        sx0 = sx1 = sx3 = sy0 = sy1 = sy3 = 0;
+    }
+    __device__ __forceinline__ void end_stage(uint32_t, uint32_t t) {
+        if ((t & 3u) == 3u) fold();
+    }
+    __device__ __forceinline__ void finish() { fold(); }
+    // the 16 totals of n particles, row-major A[j][i] (after finish)
+    __device__ __forceinline__ void totals(uint32_t n, long long (&A)[16]) const {
+        const long long one = (long long)TSCI_ONE;
+        A[0] = (long long)E[0];
+        A[1] = (long long)E[1];
+        A[3] = (long long)E[2];
+        A[4] = (long long)E[3];
+        A[5] = (long long)C11;
+        A[7] = (long long)E[4];
+        A[12] = (long long)E[5];
+        A[13] = (long long)E[6];
+        A[15] = (long long)E[7];
+        const long long sy2 = (long long)n * one - (long long)(SY0 + SY1 + SY3);
+        A[2] = one * (long long)SY0 - A[0] - A[1] - A[3];
+        A[6] = one * (long long)SY1 - A[4] - A[5] - A[7];
+        A[14] = one * (long long)SY3 - A[12] - A[13] - A[15];
+        A[8] = one * (long long)SX0 - A[0] - A[4] - A[12];
+        A[9] = one * (long long)SX1 - A[1] - A[5] - A[13];
+        A[11] = one * (long long)SX3 - A[3] - A[7] - A[15];
+        A[10] = one * sy2 - A[8] - A[9] - A[11];
+    }
+};
+
+// A particle that left its cell since the sort (out of line: rare).
+template <int S, bool QC>
+__device__ __noinline__ void stale_to_global(const DepArgs& a, uint32_t key, float rx, float ry, float qn, float vxx,
+                                             float vyy, uint32_t p) {
+    particle_to_global<S, QC>(a, key, rx, ry, qn, vxx, vyy, p);
+}
+
+// Shared memory: [stage buffers: NW warps x 2 x NF fields x LPP/4 quads x 32
+// lanes x 16 bytes][tile accumulators].
+template <int S, int LPP, int NW, bool QC, bool KEYS>
+__host__ __device__ constexpr size_t cells_fixed_bytes() {
+    return (size_t)NW * 2 * (StageFields<S, QC>::NF - (KEYS ? 0 : 1)) * (LPP / 4) * 512;
+}
+
+template <int S, int LPP, int NW, int MINB, bool QC, bool KEYS>
+__global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
+    constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
+    constexpr int NV = NX * NX;
+    constexpr int NF = StageFields<S, QC>::NF - (KEYS ? 0 : 1);  // the cell key is staged only with KEYS
+    constexpr int FX = KEYS ? 1 : 0;                            // stage field of xr
+    constexpr int FQ = FX + 2;                                  // of q (not QC)
+    constexpr int FV = FX + (QC ? 2 : 3);                       // of vx (ESK)
+    constexpr int QL = LPP / 4;                                 // quads per lane per stage
+    constexpr int BUFB = NF * QL * 512;                         // bytes of one stage buffer of a warp
+    constexpr bool TSCI = S == S_TSC && QC;                     // exact integer TSC weights
+    static_assert(LPP % 4 == 0 && LPP <= 8, "stage sums of LPP particles stay in 32 bits");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t s_count;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int SW = a.tile_w + 3;
+    const int tx = blockIdx.x % a.tiles_x, ty = blockIdx.x / a.tiles_x;
+    const int x0 = tx * a.tile_w, y0 = ty * a.tile_h;
+    const int tw = min(a.tile_w, a.Nx - x0), th = min(a.tile_h, a.Ny - y0);
+    const int nloc = (th + 3) * SW;
+    const int nch = (tw + 31) >> 5;  // units of up to 32 cells per tile row
+    unsigned char* swarp = smem_raw + (size_t)warp * 2 * BUFB;
+    const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(swarp) + (uint32_t)(lane * 16);
+    uint32_t* slo = reinterpret_cast<uint32_t*>(smem_raw + cells_fixed_bytes<S, LPP, NW, QC, KEYS>());
+    int* shi = reinterpret_cast<int*>(slo + nloc);
+    if (threadIdx.x == 0) s_count = 0;
+    for (int i = threadIdx.x; i < nloc; i += NW * 32) {
+        slo[i] = 0;
+        shi[i] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x < th) {
+        const uint32_t c0 = (uint32_t)(y0 + threadIdx.x) * (uint32_t)a.Nx + (uint32_t)x0;
+        atomicAdd(&s_count, a.offsets[c0 + tw] - a.offsets[c0]);
+    }
+    __syncthreads();
+    const bool dense = s_count >= TILE_SPLIT_MAX;
+
+    const uint32_t* fptr[NF];
+    if constexpr (KEYS) fptr[0] = a.cell;
+    fptr[FX] = reinterpret_cast<const uint32_t*>(a.xr);
+    fptr[FX + 1] = reinterpret_cast<const uint32_t*>(a.yr);
+    if constexpr (!QC) fptr[FQ] = reinterpret_cast<const uint32_t*>(a.q);
+    if constexpr (S == S_ESK) {
+        fptr[FV] = reinterpret_cast<const uint32_t*>(a.vx);
+        fptr[FV + 1] = reinterpret_cast<const uint32_t*>(a.vy);
+    }
+    // unit u = (tile row, 32-cell chunk); this lane's cell range and quads
+    struct Unit {
+        uint32_t beg, end, q0, q1, nst;  // particles [beg, end), quads [q0, q1), stages of the unit
+        int r, col;                     // tile row, this lane's column in the tile (-1: no cell)
+    };
+    const int nunits = th * nch;
+    auto unit_of = [&](int u) {
+        Unit w;
+        w.r = u / nch;
+        const int col = (u - w.r * nch) * 32 + lane;
+        w.col = col < tw ? col : -1;
+        w.beg = w.end = 0;
+        if (w.col >= 0) {
+            const uint32_t c = (uint32_t)(y0 + w.r) * (uint32_t)a.Nx + (uint32_t)(x0 + w.col);
+            w.beg = a.offsets[c];
+            w.end = a.offsets[c + 1];
+        }
+        w.q0 = w.beg >> 2;
+        w.q1 = w.end > w.beg ? (w.end + 3u) >> 2 : w.q0;
+        const uint32_t st = (w.q1 - w.q0 + QL - 1) / QL;
+        w.nst = __reduce_max_sync(FULL, st);
+        return w;
+    };
+    auto issue = [&](const Unit& w, uint32_t t, int buf) {
+        const uint32_t dst = stage0 + (uint32_t)(buf * BUFB);
+#pragma unroll
+        for (int h = 0; h < QL; ++h) {
+            const uint32_t qd = w.q0 + t * QL + (uint32_t)h;
+            if (qd < w.q1) {
+#pragma unroll
+                for (int f = 0; f < NF; ++f) cp_async16(dst + (uint32_t)((f * QL + h) * 512), fptr[f] + 4u * qd);
+            }
+        }
+        cp_async_commit();
+    };
+
+    int u = warp;
+    Unit cw{};
+    while (u < nunits) {
+        cw = unit_of(u);
+        if (cw.nst) break;
+        u += NW;
+    }
+    if (u < nunits) issue(cw, 0u, 0);
+    uint32_t t = 0;
+    int buf = 0;
+    uint32_t cnt = 0;  // particles of the cell summed (KEYS: those still in it)
+    CellRun<S, QC> run;
+    run.zero();
+    while (u < nunits) {
+        // the stage after this one: next stage of this unit or first of the next non-empty unit
+        int un = u;
+        uint32_t tn = t + 1;
+        Unit nw = cw;
+        if (tn >= cw.nst) {
+            tn = 0;
+            nw.nst = 0;
+            for (un = u + NW; un < nunits; un += NW) {
+                nw = unit_of(un);
+                if (nw.nst) break;
+            }
+        }
+        if (un < nunits) {
+            issue(nw, tn, buf ^ 1);
+        } else {
+            cp_async_commit();
+        }
+        cp_async_wait_1();
+        __syncwarp();
+
+        const int iy = y0 + cw.r;
+        const uint32_t rowbase = (uint32_t)iy * (uint32_t)a.Nx;
+        const uint32_t mykey = rowbase + (uint32_t)(x0 + cw.col);
+        const unsigned char* sb = swarp + (size_t)buf * BUFB + lane * 16;
+        uint32_t scnt = 0;  // particles summed in this stage
+#pragma unroll
+        for (int h = 0; h < QL; ++h) {
+            const uint32_t qd = cw.q0 + t * QL + (uint32_t)h;
+            if (qd < cw.q1) {
+                Quad<S> d;
+                if constexpr (KEYS) d.cell = *reinterpret_cast<const uint4*>(sb + h * 512);
+                d.xr = *reinterpret_cast<const float4*>(sb + (FX * QL + h) * 512);
+                d.yr = *reinterpret_cast<const float4*>(sb + ((FX + 1) * QL + h) * 512);
+                if constexpr (QC)
+                    d.q = make_float4(a.qc, a.qc, a.qc, a.qc);
+                else
+                    d.q = *reinterpret_cast<const float4*>(sb + (FQ * QL + h) * 512);
+                if constexpr (S == S_ESK) {
+                    d.vx = *reinterpret_cast<const float4*>(sb + (FV * QL + h) * 512);
+                    d.vy = *reinterpret_cast<const float4*>(sb + ((FV + 1) * QL + h) * 512);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t p = 4u * qd + (uint32_t)k;
+                    if (p - cw.beg < cw.end - cw.beg) {
+                        float vxx = 0.0f, vyy = 0.0f;
+                        if constexpr (S == S_ESK) {
+                            vxx = f4(d.vx, k);
+                            vyy = f4(d.vy, k);
+                        }
+                        if constexpr (KEYS) {
+                            const uint32_t key = u4(d.cell, k);
+                            if (key != mykey) {  // left its cell since the last sort
+                                stale_to_global<S, QC>(a, key, f4(d.xr, k), f4(d.yr, k), f4(d.q, k), vxx, vyy, p);
+                                continue;
+                            }
+                        }
+                        if constexpr (TSCI) {
+                            run.add(f4(d.xr, k), f4(d.yr, k));
+                        } else if constexpr (S == S_TSC) {
+                            tsc_accumulate(f4(d.xr, k), f4(d.yr, k), f4(d.q, k), run.v);
+                        } else {
+                            int iv[V];
+                            if (!stencil_values<S>(a, f4(d.xr, k), f4(d.yr, k), f4(d.q, k), vxx, vyy,
+                                                   (int)(mykey - rowbase), iy, p, iv))
+                                continue;  // deposited by the general trajectory path
+#pragma unroll
+                            for (int q = 0; q < NV; ++q) run.v[q] += (uint32_t)iv[q];
+                        }
+                        ++scnt;
+                    }
+                }
+                run.end_quad();
+            }
+        }
+        run.end_stage(scnt, t);
+        cnt += scnt;
+        if (tn == 0) {  // the end of the unit: write out this lane's cell
+            if (cnt) {
+                long long tv[NV];
+                run.finish();
+                run.totals(cnt, tv);
+                if (dense) {
+                    flush_global_ll<NX, LO, NV>(a, mykey, tv);
+                } else {
+                    const int lx = cw.col + 1 + LO;
+                    const int lrow = cw.r + 1 + LO;
+#pragma unroll
+                    for (int q = 0; q < NV; ++q) {
+                        const long long x = tv[q];
+                        if (x != 0) {
+                            const int i = (lrow + q / NX) * SW + lx + (q % NX);
+                            atomicAdd(slo + i, (uint32_t)x & ((1u << TILE_SPLIT) - 1u));
+                            atomicAdd(shi + i, (int)(x >> TILE_SPLIT));
+                        }
+                    }
+                }
+            }
+            run.zero();
+            cnt = 0;
+        }
+        __syncwarp();
+        u = un;
+        t = tn;
+        cw = nw;
+        buf ^= 1;
+    }
+    __syncthreads();
+    if (dense) return;
+    for (int i = threadIdx.x; i < nloc; i += NW * 32) {
+        // the high word is signed in the general form, unsigned in the exact integer TSC form
+        const long long hi = TSCI ? (long long)(uint32_t)shi[i] : (long long)shi[i];
+        const long long v = hi * (1ll << TILE_SPLIT) + (long long)slo[i];
+        if (v != 0) {
+            const int ly = i / SW, lx = i % SW;
+            const int gx = wrap_i(x0 - 1 + lx, a.Nx), gy = wrap_i(y0 - 1 + ly, a.Ny);
+            atomicAdd(a.acc + (size_t)gy * a.Nx + gx, (unsigned long long)v);
+        }
+    }
+}
+
+// One unit of the int64 grid (FP64): max|q| * inv_vol * 2^-24, or, for the
+// exact integer TSC form, max|q| * inv_vol * (qn * 2^-30) (scale != 0).
+__global__ void fixed_unit(double inv_vol, double scale, const DevStats* st, double* unit_out) {
+    *unit_out = scale == 0.0 ? charge_unit(st, inv_vol) : __dmul_rn(__dmul_rn((double)load_maxq(st), inv_vol), scale);
 }
 
 __global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double background,
@@ -1012,14 +1339,13 @@ __global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double
     if (i < g) rho[i] = __dadd_rn(__dmul_rn((double)acc[i], unit), background);
 }
 
-template <int S, int LPP, int NW, int MINB, bool QC>
-static int launch_tiled(pic_ctx* c, const DepArgs& a, unsigned tiles) {
-    const size_t smem =
-        tiled_fixed_bytes<S, LPP, NW, QC>() + (size_t)(a.tile_h + 3) * (a.tile_w + 3) * 2 * sizeof(uint32_t);
-    // dynamic shared memory above 48 KB must be opted into
-    const int rc = opt_in_dynamic_smem((const void*)deposit_tiled<S, LPP, NW, MINB, QC>, smem);
+template <int S, int LPP, int NW, int MINB, bool QC, bool KEYS>
+static int launch_cells(pic_ctx* c, const DepArgs& a, unsigned tiles) {
+    const size_t smem = cells_fixed_bytes<S, LPP, NW, QC, KEYS>() +
+                        (size_t)(a.tile_h + 3) * (a.tile_w + 3) * 2 * sizeof(uint32_t);
+    const int rc = opt_in_dynamic_smem((const void*)deposit_cells<S, LPP, NW, MINB, QC, KEYS>, smem);
     if (rc != PIC_OK) return rc;
-    deposit_tiled<S, LPP, NW, MINB, QC><<<tiles, NW * 32, smem, c->stream>>>(a);
+    deposit_cells<S, LPP, NW, MINB, QC, KEYS><<<tiles, NW * 32, smem, c->stream>>>(a);
     return PIC_OK;
 }
 
@@ -1033,14 +1359,19 @@ static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
         // registers (5 CTAs per SM), measured fastest at 1024^2 x 64 particles/cell.
         // cp.async staging measured 10 % faster than TMA tensor copies of the
         // same stages (128-byte swizzle, one lane issuing, mbarrier completion)
+        // freshly sorted: the offsets name every particle's cell and the keys are not read
+        const bool keys = !c->sorted;
         int rc;
-        if (a.qc != 0.0f)  // one charge for all particles: the charge stream is not staged
-            rc = launch_tiled<S, 8, 4, S == S_TSC ? 5 : 4, true>(c, a, tiles);
-        else
-            rc = launch_tiled<S, 8, 4, S == S_TSC ? 5 : 4, false>(c, a, tiles);
+        if (a.qc != 0.0f) {  // one charge for all particles: the charge stream is not staged
+            rc = keys ? launch_cells<S, 8, 4, 4, true, true>(c, a, tiles)
+                      : launch_cells<S, 8, 4, 4, true, false>(c, a, tiles);
+        } else {
+            rc = keys ? launch_cells<S, 8, 4, 4, false, true>(c, a, tiles)
+                      : launch_cells<S, 8, 4, 4, false, false>(c, a, tiles);
+        }
         prof_end(c);
         if (rc != PIC_OK) return rc;
-        return check_launch(c, "deposit_tiled");
+        return check_launch(c, "deposit_cells");
     }
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
@@ -1050,9 +1381,12 @@ static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
         if (blocks > cap) blocks = cap;
         if (blocks == 0) blocks = 1;
         prof_begin(c, "deposit");
-        if constexpr (S == S_TSC)
-            deposit_runs_tsc<<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
-        else
+        if constexpr (S == S_TSC) {
+            if (a.qc != 0.0f)
+                deposit_runs_tsci<<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
+            else
+                deposit_runs_tsc<<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
+        } else
             deposit_runs<S><<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
         prof_end(c);
         return check_launch(c, "deposit_runs");
@@ -1100,11 +1434,11 @@ int deposit_rho(pic_ctx* c, int scheme, double dt, double background) {
     a.dtdx = (float)(dt / c->dx);
     a.dtdy = (float)(dt / c->dy);
     if (!c->tile_user) {
-        // about 8K particles per tile (measured best at 16 and 64 particles per
-        // cell), at least as many rows as the 4 warps of a CTA
+        // rows of 32 cells (one per lane) and about 8K particles per tile, at
+        // least as many rows as the 4 warps of a CTA
         const double ppc = (double)c->n / (double)c->G;
         const double cells = ppc > 0.0 ? 8192.0 / ppc : 2048.0;
-        c->tile_w = cells <= 256.0 ? 32 : 64;
+        c->tile_w = 32;
         int h = 4;
         while (h < 32 && (double)(c->tile_w * h * 2) <= cells) h *= 2;
         c->tile_h = h;
@@ -1131,7 +1465,11 @@ int deposit_rho(pic_ctx* c, int scheme, double dt, double background) {
         }
     }
     const double inv_vol = 1.0 / (c->dx * c->dy);
-    fixed_unit<<<1, 1, 0, c->stream>>>(inv_vol, c->dstats, c->unitbuf);
+    // TSC with one charge for all particles deposits exact integer weights (2^30 units per particle)
+    const double scale = (scheme == PIC_SCHEME_TSC && c->n > 0 && c->qn_uniform != 0.0f)
+                             ? (double)c->qn_uniform * 0x1p-30
+                             : 0.0;
+    fixed_unit<<<1, 1, 0, c->stream>>>(inv_vol, scale, c->dstats, c->unitbuf);
     PIC_TRY(check_launch(c, "fixed_unit"));
     fixed_to_rho<<<(unsigned)((c->G + 255) / 256), 256, 0, c->stream>>>(c->acc, c->G, background, c->unitbuf,
                                                                          c->rho);

@@ -184,8 +184,44 @@ def test_fixed_point_restatement_close_to_fp64(port, scheme):
     rel = np.linalg.norm(got - want) / np.linalg.norm(want)
     assert rel < 1e-6
     # every particle deposits exactly its integer charge, so the grid total is exact
-    assert acc.sum() == int(np.sum(np.rint(qn.astype(np.float64) * 2 ** 24)))
+    assert acc.sum() == port.fixed_total(scheme, qn)
     assert abs(acc.sum() * unit - p["q"].sum()) <= 1e-12 * np.abs(p["q"]).sum()
+
+
+def test_tsc_one_charge_exact_integer_form(port):
+    """One charge for every particle: TSC deposits exact integer weights (each axis'
+    three weights rounded to 2^-15 and summing to 2^15 exactly). On the benchmark's
+    density (1 + 0.01 cos, 64 particles per cell, a 128x128 slice) rho stays within
+    3e-6 relative L2 of the reference-pinned FP64 deposit, a third of the 1e-5 gate,
+    and the grid total is exactly n * 2^30 units (the charge sits in the unit)."""
+    import workloads
+
+    nx = ny = 128
+    p = workloads.density_cos(nx, ny, 64, 0.01, 0.1, seed=5)
+    n = len(p["x"])
+    cell, xr, yr = port.to_device(nx, ny, float(nx), float(ny), p["x"], p["y"])
+    qn, maxq = port.normalize_charge(p["q"])
+    assert port.charge_uniform(qn) and not port.charge_uniform(np.where(np.arange(n) == 7, 1, -1).astype(np.float32))
+    acc, unit = port.deposit_fixed(nx, ny, float(nx), float(ny), TSC, cell, xr, yr, qn, maxq)
+    assert unit == -2.0 ** -30 and acc.min() >= 0
+    assert acc.sum() == port.fixed_total(TSC, qn) == n << 30
+    want = port.deposit_ref(nx, ny, float(nx), float(ny), TSC, p, threads=4)
+    rel = np.linalg.norm(acc * unit - want) / np.linalg.norm(want)
+    assert rel <= 3e-6, rel
+    # one particle at a time: its 16 frame values are WX[i] * WY[j] with each axis summing to 2^15
+    for r in (0.0, 0.25, 0.5 - 2 ** -24, 0.5, 0.75, 1.0 - 2 ** -24):
+        one_c, one_x, one_y = np.array([5 * 16 + 5], np.uint32), np.array([r], np.float32), np.array([0.5], np.float32)
+        a1, _ = port.deposit_fixed(16, 16, 16.0, 16.0, TSC, one_c, one_x, one_y, np.array([1.0], np.float32), 1.0)
+        g = a1.reshape(16, 16)
+        wy = g.sum(axis=1)  # a row's sum is 2^15 * WY[j]
+        wx = g.sum(axis=0)
+        assert wy.sum() == 2 ** 30 and np.all(wy % 2 ** 15 == 0) and np.all(wx % 2 ** 15 == 0)
+        xi = 5.0 + r
+        i0 = int(np.floor(xi - 0.5))
+        t = xi - i0
+        w = np.array([0.5 * (1.5 - t) ** 2, 0.75 - (t - 1) ** 2, 0.5 * (t - 0.5) ** 2])
+        got = wx[i0:i0 + 3] / 2.0 ** 30
+        assert np.max(np.abs(got - w)) <= 2.0 ** -15, (r, got, w)
 
 
 def test_to_device_keeps_ngp_choice(port):
