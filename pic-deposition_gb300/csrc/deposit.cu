@@ -793,7 +793,10 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 // Adds a run's exact integer TSC totals for cell `key` straight to the global
 // grid, without integer division (as flush_global_nd).
@@ -983,8 +986,8 @@ struct CellRun {
     }
     __device__ __forceinline__ void end_quad() {}
     __device__ __forceinline__ void finish() {}
-    // adds the sums of stage t (`cnt` particles) to the totals
-    __device__ __forceinline__ void end_stage(uint32_t cnt, uint32_t) {
+    // adds the sums of a stage (`cnt` particles) to the totals
+    __device__ __forceinline__ void end_stage(uint32_t cnt, bool) {
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
             if constexpr (S == S_TSC)
@@ -1008,9 +1011,9 @@ struct CellRun {
 // follow exactly (integer identities) when the cell is written out. Per
 // particle: 9 32-bit multiply-adds and 6 adds. Bounds: the 8 entries other than
 // A[1][1] are at most 2^12 * 24576 < 2^26.6 per particle, summed in 32 bits for
-// 4 stages (at most 32 particles) and then added to 64-bit totals; A[1][1] <=
+// at most 32 particles (32/LPP stages) and then added to 64-bit totals; A[1][1] <=
 // 24576^2 < 2^29.2 per particle is summed in 32 bits for a quad (4 particles);
-// the axis sums are 64-bit totals of 32-bit sums of 4 stages.
+// the axis sums are 64-bit totals of 32-bit sums of as many stages.
 template <>
 struct CellRun<S_TSC, true> {
     static constexpr int NV = 16;
@@ -1067,8 +1070,8 @@ struct CellRun<S_TSC, true> {
         SY3 += sy3;
         sx0 = sx1 = sx3 = sy0 = sy1 = sy3 = 0;
     }
-    __device__ __forceinline__ void end_stage(uint32_t, uint32_t t) {
-        if ((t & 3u) == 3u) fold();
+    __device__ __forceinline__ void end_stage(uint32_t, bool fold_now) {
+        if (fold_now) fold();
     }
     __device__ __forceinline__ void finish() { fold(); }
     // the 16 totals of n particles, row-major A[j][i] (after finish)
@@ -1094,6 +1097,35 @@ struct CellRun<S_TSC, true> {
     }
 };
 
+// NGP with one charge for all particles: every particle deposits exactly
+// A = rint(qn * 2^24) units to its nearest node (ngp.cpp:108-120, ties go up),
+// so a cell's four node sums are A times the counts of its particles in each
+// quarter of the cell: the general form's values bit for bit, from two
+// comparisons and three counts per particle.
+template <>
+struct CellRun<S_NGP, true> {
+    static constexpr int NV = 4;
+    int A;                 // the units of one particle
+    uint32_t nx, ny, nxy;  // particles with rx >= 0.5, ry >= 0.5, both
+    __device__ __forceinline__ void zero() { nx = ny = nxy = 0; }
+    __device__ __forceinline__ void add(float rx, float ry) {
+        const uint32_t sx = rx >= 0.5f ? 1u : 0u, sy = ry >= 0.5f ? 1u : 0u;
+        nx += sx;
+        ny += sy;
+        nxy += sx & sy;
+    }
+    __device__ __forceinline__ void end_quad() {}
+    __device__ __forceinline__ void end_stage(uint32_t, bool) {}
+    __device__ __forceinline__ void finish() {}
+    __device__ __forceinline__ void totals(uint32_t n, long long (&T)[4]) const {
+        const long long a = A;
+        T[0] = a * ((long long)n - nx - ny + nxy);
+        T[1] = a * ((long long)nx - nxy);
+        T[2] = a * ((long long)ny - nxy);
+        T[3] = a * (long long)nxy;
+    }
+};
+
 // A particle that left its cell since the sort (out of line: rare).
 template <int S, bool QC>
 __device__ __noinline__ void stale_to_global(const DepArgs& a, uint32_t key, float rx, float ry, float qn, float vxx,
@@ -1101,14 +1133,15 @@ __device__ __noinline__ void stale_to_global(const DepArgs& a, uint32_t key, flo
     particle_to_global<S, QC>(a, key, rx, ry, qn, vxx, vyy, p);
 }
 
-// Shared memory: [stage buffers: NW warps x 2 x NF fields x LPP/4 quads x 32
-// lanes x 16 bytes][tile accumulators].
-template <int S, int LPP, int NW, bool QC, bool KEYS>
+// Shared memory: [stage buffers: NW warps x NBUF x NF fields x LPP/4 quads x
+// 32 lanes x 16 bytes][tile accumulators: low, high words][the tile rows' cell
+// offsets].
+template <int S, int LPP, int NW, bool QC, bool KEYS, int NBUF>
 __host__ __device__ constexpr size_t cells_fixed_bytes() {
-    return (size_t)NW * 2 * (StageFields<S, QC>::NF - (KEYS ? 0 : 1)) * (LPP / 4) * 512;
+    return (size_t)NW * NBUF * (StageFields<S, QC>::NF - (KEYS ? 0 : 1)) * (LPP / 4) * 512;
 }
 
-template <int S, int LPP, int NW, int MINB, bool QC, bool KEYS>
+template <int S, int LPP, int NW, int MINB, bool QC, bool KEYS, int NBUF>
 __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
     constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
     constexpr int NV = NX * NX;
@@ -1119,7 +1152,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
     constexpr int QL = LPP / 4;                                 // quads per lane per stage
     constexpr int BUFB = NF * QL * 512;                         // bytes of one stage buffer of a warp
     constexpr bool TSCI = S == S_TSC && QC;                     // exact integer TSC weights
-    static_assert(LPP % 4 == 0 && LPP <= 8, "stage sums of LPP particles stay in 32 bits");
+    static_assert(LPP % 4 == 0 && LPP <= 16, "stage sums of LPP particles stay in 32 bits");
+    constexpr uint32_t FOLD = 32 / LPP;  // stages per fold of the exact TSC partial sums (32 particles)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint32_t s_count;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1129,20 +1163,23 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
     const int tw = min(a.tile_w, a.Nx - x0), th = min(a.tile_h, a.Ny - y0);
     const int nloc = (th + 3) * SW;
     const int nch = (tw + 31) >> 5;  // units of up to 32 cells per tile row
-    unsigned char* swarp = smem_raw + (size_t)warp * 2 * BUFB;
+    unsigned char* swarp = smem_raw + (size_t)warp * NBUF * BUFB;
     const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(swarp) + (uint32_t)(lane * 16);
-    uint32_t* slo = reinterpret_cast<uint32_t*>(smem_raw + cells_fixed_bytes<S, LPP, NW, QC, KEYS>());
+    uint32_t* slo = reinterpret_cast<uint32_t*>(smem_raw + cells_fixed_bytes<S, LPP, NW, QC, KEYS, NBUF>());
     int* shi = reinterpret_cast<int*>(slo + nloc);
+    uint32_t* soff = reinterpret_cast<uint32_t*>(shi + nloc);  // the tile rows' offsets, th x (tw + 1)
+    const int ow = tw + 1;
     if (threadIdx.x == 0) s_count = 0;
     for (int i = threadIdx.x; i < nloc; i += NW * 32) {
         slo[i] = 0;
         shi[i] = 0;
     }
-    __syncthreads();
-    if (threadIdx.x < th) {
-        const uint32_t c0 = (uint32_t)(y0 + threadIdx.x) * (uint32_t)a.Nx + (uint32_t)x0;
-        atomicAdd(&s_count, a.offsets[c0 + tw] - a.offsets[c0]);
+    for (int i = threadIdx.x; i < th * ow; i += NW * 32) {
+        const int r = i / ow;
+        soff[i] = a.offsets[(uint32_t)(y0 + r) * (uint32_t)a.Nx + (uint32_t)x0 + (uint32_t)(i - r * ow)];
     }
+    __syncthreads();
+    if (threadIdx.x < th) atomicAdd(&s_count, soff[threadIdx.x * ow + tw] - soff[threadIdx.x * ow]);
     __syncthreads();
     const bool dense = s_count >= TILE_SPLIT_MAX;
 
@@ -1168,9 +1205,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
         w.col = col < tw ? col : -1;
         w.beg = w.end = 0;
         if (w.col >= 0) {
-            const uint32_t c = (uint32_t)(y0 + w.r) * (uint32_t)a.Nx + (uint32_t)(x0 + w.col);
-            w.beg = a.offsets[c];
-            w.end = a.offsets[c + 1];
+            w.beg = soff[w.r * ow + w.col];
+            w.end = soff[w.r * ow + w.col + 1];
         }
         w.q0 = w.beg >> 2;
         w.q1 = w.end > w.beg ? (w.end + 3u) >> 2 : w.q0;
@@ -1191,39 +1227,44 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
         cp_async_commit();
     };
 
-    int u = warp;
+    // the first non-empty unit at or after u (nunits: none)
+    auto next_unit = [&](int u, Unit& w) {
+        for (; u < nunits; u += NW) {
+            w = unit_of(u);
+            if (w.nst) break;
+        }
+        return u;
+    };
+    // prefetch cursor (stage pt of unit pu), NBUF - 1 stages ahead of the consumer
+    Unit pw{};
+    int pu = next_unit(warp, pw);
+    uint32_t pt = 0;
+    auto issue_next = [&](int buf) {
+        if (pu < nunits) {
+            issue(pw, pt, buf);
+            if (++pt >= pw.nst) {
+                pt = 0;
+                pu = next_unit(pu + NW, pw);
+            }
+        } else {
+            cp_async_commit();  // an empty group keeps the wait counts uniform
+        }
+    };
+#pragma unroll
+    for (int k = 0; k < NBUF - 1; ++k) issue_next(k);
     Unit cw{};
-    while (u < nunits) {
-        cw = unit_of(u);
-        if (cw.nst) break;
-        u += NW;
-    }
-    if (u < nunits) issue(cw, 0u, 0);
+    int u = next_unit(warp, cw);
     uint32_t t = 0;
     int buf = 0;
     uint32_t cnt = 0;  // particles of the cell summed (KEYS: those still in it)
     CellRun<S, QC> run;
+    if constexpr (S == S_NGP && QC) run.A = __float2int_rn(a.qc * 16777216.0f);
     run.zero();
     while (u < nunits) {
-        // the stage after this one: next stage of this unit or first of the next non-empty unit
-        int un = u;
-        uint32_t tn = t + 1;
-        Unit nw = cw;
-        if (tn >= cw.nst) {
-            tn = 0;
-            nw.nst = 0;
-            for (un = u + NW; un < nunits; un += NW) {
-                nw = unit_of(un);
-                if (nw.nst) break;
-            }
-        }
-        if (un < nunits) {
-            issue(nw, tn, buf ^ 1);
-        } else {
-            cp_async_commit();
-        }
-        cp_async_wait_1();
+        issue_next(buf == 0 ? NBUF - 1 : buf - 1);  // the buffer consumed last
+        cp_async_wait<NBUF - 1>();
         __syncwarp();
+        const bool unit_end = t + 1 >= cw.nst;
 
         const int iy = y0 + cw.r;
         const uint32_t rowbase = (uint32_t)iy * (uint32_t)a.Nx;
@@ -1262,7 +1303,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
                                 continue;
                             }
                         }
-                        if constexpr (TSCI) {
+                        if constexpr (TSCI || (S == S_NGP && QC)) {
                             run.add(f4(d.xr, k), f4(d.yr, k));
                         } else if constexpr (S == S_TSC) {
                             tsc_accumulate(f4(d.xr, k), f4(d.yr, k), f4(d.q, k), run.v);
@@ -1280,9 +1321,9 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
                 run.end_quad();
             }
         }
-        run.end_stage(scnt, t);
+        run.end_stage(scnt, (t + 1u) % FOLD == 0u);
         cnt += scnt;
-        if (tn == 0) {  // the end of the unit: write out this lane's cell
+        if (unit_end) {  // the end of the unit: write out this lane's cell
             if (cnt) {
                 long long tv[NV];
                 run.finish();
@@ -1307,11 +1348,15 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
             cnt = 0;
         }
         __syncwarp();
-        u = un;
-        t = tn;
-        cw = nw;
-        buf ^= 1;
+        if (unit_end) {
+            t = 0;
+            u = next_unit(u + NW, cw);
+        } else {
+            ++t;
+        }
+        buf = buf + 1 == NBUF ? 0 : buf + 1;
     }
+    cp_async_wait<0>();
     __syncthreads();
     if (dense) return;
     for (int i = threadIdx.x; i < nloc; i += NW * 32) {
@@ -1339,13 +1384,21 @@ __global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double
     if (i < g) rho[i] = __dadd_rn(__dmul_rn((double)acc[i], unit), background);
 }
 
+#ifndef CELLS_LPP
+#define CELLS_LPP 8
+#endif
+#ifndef CELLS_NBUF
+#define CELLS_NBUF 2
+#endif
 template <int S, int LPP, int NW, int MINB, bool QC, bool KEYS>
 static int launch_cells(pic_ctx* c, const DepArgs& a, unsigned tiles) {
-    const size_t smem = cells_fixed_bytes<S, LPP, NW, QC, KEYS>() +
-                        (size_t)(a.tile_h + 3) * (a.tile_w + 3) * 2 * sizeof(uint32_t);
-    const int rc = opt_in_dynamic_smem((const void*)deposit_cells<S, LPP, NW, MINB, QC, KEYS>, smem);
+    constexpr int NBUF = CELLS_NBUF;
+    const size_t smem = cells_fixed_bytes<S, LPP, NW, QC, KEYS, NBUF>() +
+                        (size_t)(a.tile_h + 3) * (a.tile_w + 3) * 2 * sizeof(uint32_t) +
+                        (size_t)a.tile_h * (a.tile_w + 1) * sizeof(uint32_t);
+    const int rc = opt_in_dynamic_smem((const void*)deposit_cells<S, LPP, NW, MINB, QC, KEYS, NBUF>, smem);
     if (rc != PIC_OK) return rc;
-    deposit_cells<S, LPP, NW, MINB, QC, KEYS><<<tiles, NW * 32, smem, c->stream>>>(a);
+    deposit_cells<S, LPP, NW, MINB, QC, KEYS, NBUF><<<tiles, NW * 32, smem, c->stream>>>(a);
     return PIC_OK;
 }
 
@@ -1363,11 +1416,11 @@ static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
         const bool keys = !c->sorted;
         int rc;
         if (a.qc != 0.0f) {  // one charge for all particles: the charge stream is not staged
-            rc = keys ? launch_cells<S, 8, 4, 4, true, true>(c, a, tiles)
-                      : launch_cells<S, 8, 4, 4, true, false>(c, a, tiles);
+            rc = keys ? launch_cells<S, CELLS_LPP, 4, 4, true, true>(c, a, tiles)
+                      : launch_cells<S, CELLS_LPP, 4, 4, true, false>(c, a, tiles);
         } else {
-            rc = keys ? launch_cells<S, 8, 4, 4, false, true>(c, a, tiles)
-                      : launch_cells<S, 8, 4, 4, false, false>(c, a, tiles);
+            rc = keys ? launch_cells<S, CELLS_LPP, 4, 4, false, true>(c, a, tiles)
+                      : launch_cells<S, CELLS_LPP, 4, 4, false, false>(c, a, tiles);
         }
         prof_end(c);
         if (rc != PIC_OK) return rc;
