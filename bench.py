@@ -7,19 +7,24 @@ velocities vth = 0.1, charge -1, seeded synthetic data. The particles are
 cell-sorted once before timing.
 
 One step = one CIC charge deposition of all particles into an FP64 rho grid
-(clear + tiled fixed-point deposit + conversion), particles resident in HBM.
-The particle stream (0.81 GB: cell, xr, yr, as every particle has the same charge;
-1.07 GB with per-particle charges) is far larger than L2 (129 MB), so no L2 flush
-is needed between steps.
+(clear + sorted fixed-point deposit + conversion), particles resident in HBM.
+The sorted deposit reads each particle's in-cell offsets xr, yr (and its charge
+when charges differ); the per-cell offsets name every particle's cell, so the
+cell keys are not read: 0.54 GB per step (8 B per particle, every particle has
+the same charge), far larger than L2 (129 MB), so no L2 flush is needed.
 
   value   particles/s over the timed steps (CUDA events on the library stream),
           summed over ranks (replicas; one GPU each), max time over ranks.
   e2e     the same metric through the public C ABI with host buffers: every
           step uploads x, y, q (FP64, pinned) and downloads rho (FP64).
-  roofline  the deposit kernel alone: algorithmic bytes (12 B per particle
+  roofline  the deposit kernel alone: algorithmic bytes (8 B per particle
           when every particle has the same charge, as here -- the charge stream
-          is not read -- else 16 B; + 8 B per cell) / its mean CUDA-event
-          duration, against the measured HBM copy bandwidth in MEASURED_PEAKS.json.
+          is not read -- else 12 B; + 12 B per cell: the int64 grid written, the
+          cell offsets read) / its mean CUDA-event duration, against the measured
+          HBM copy bandwidth in MEASURED_PEAKS.json.
+  summary   last on the line: per-kernel times and fractions of HBM, the
+          per-scheme errors against the FP64 deposit, and the time-step,
+          ensemble, warm-start and convolution headlines, rounded.
   cpu_baseline  the reference's FP64 CPU deposit on the host cores (rank 0);
           its "detail" times every scheme at 1 and at all host threads, and the
           reference's cell sort where it is built, on a 4 M-particle sample.
@@ -51,12 +56,17 @@ AMP = 0.01
 VTH = 0.1
 ESK_DT = 0.1
 SCHEMES = {"NGP": 0, "CIC": 1, "TSC": 2, "Esirkepov": 3}
-BYTES_PER_PARTICLE = 16  # x_rel, y_rel, q (FP32) + cell key (u32)
-BYTES_PER_PARTICLE_ESK = 24  # + vx, vy
+# Algorithmic bytes of the sorted deposit: a cell-sorted particle set is read as
+# its in-cell offsets x_rel, y_rel (FP32) and charge q (FP32) -- the per-cell
+# offsets array (4 B per cell) names every particle's cell, so the cell keys are
+# not read -- plus vx, vy for the Esirkepov schemes; the int64 grid is written
+# once (8 B per cell).
+BYTES_PER_PARTICLE = 12  # x_rel, y_rel, q (FP32)
+BYTES_PER_PARTICLE_ESK = 20  # + vx, vy
 # with one charge for every particle (the workloads here: q = -1) the kernels
 # do not read the charge stream: 4 B less per particle
 BYTES_Q = 4
-BYTES_PER_CELL = 8  # int64 rho written once
+BYTES_PER_CELL = 12  # int64 rho written once + the u32 cell offsets read once
 # learned warm start for red-black Gauss-Seidel: 512x512, 64 particles per cell,
 # density 1 + 0.05*cos(2*pi*x/512), vth = 1 (the reference's charge convention,
 # total charge -1 and m = 1, with the neutralising background), dt = 0.1
@@ -121,7 +131,7 @@ def peaks():
 
 def traffic_from_profile():
     """dram bytes per deposit launch from the committed ncu summary (None if absent)."""
-    path = os.path.join(ROOT, "profiles", "deposit_tiled_cic_1024x1024_64ppc.txt")
+    path = os.path.join(ROOT, "profiles", "deposit_cells_cic_1024x1024_64ppc.txt")
     if not os.path.exists(path):
         return None
     with open(path) as f:
@@ -317,6 +327,65 @@ def cpu_detail(ps, threads_all: int, sample: int = 4_000_000):
     return out
 
 
+def fp64_errors(p, gpu_out, threads):
+    """Max-abs and relative L2 of the GPU's rho per scheme (and of the Esirkepov
+    current Jx, Jy) against the reference's FP64 deposit of the same particles
+    (the oracle's restatement of src/deposition/ngp.cpp, pinned bit for bit to the
+    reference; the FP64 Esirkepov-2001 current), computed by the CPU-baseline leg."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    port = oracle.Port()
+    out = {}
+    for nm, code in SCHEMES.items():
+        ref = port.deposit_ref(NX, NY, float(NX), float(NY), code, p, dt=ESK_DT, threads=threads)
+        d = gpu_out[nm] - ref
+        out["ESK_rho" if nm == "Esirkepov" else nm] = {"max_abs": float(np.max(np.abs(d))),
+                                                       "rel_l2": float(np.linalg.norm(d) / np.linalg.norm(ref)),
+                                                       "ref_max_abs": float(np.max(np.abs(ref)))}
+    jx, jy = port.esirkepov_j_ref(NX, NY, float(NX), float(NY), p, ESK_DT)
+    for nm, ref in (("Jx", jx), ("Jy", jy)):
+        d = gpu_out[nm] - ref
+        out[nm] = {"max_abs": float(np.max(np.abs(d))), "rel_l2": float(np.linalg.norm(d) / np.linalg.norm(ref)),
+                   "ref_max_abs": float(np.max(np.abs(ref)))}
+    out["workload"] = f"{WORKLOAD} (all particles), dt {ESK_DT} for the Esirkepov schemes"
+    return out
+
+
+def r4(x):
+    """x rounded to 4 significant digits (None stays None)."""
+    if x is None:
+        return None
+    return float(f"{x:.4g}")
+
+
+def summary(res):
+    """The figures a reader needs, compact, at the end of the line (the part a log tail keeps)."""
+    ex = res.get("extra") or {}
+    out = {"kernels": {}}
+    for k, v in ex.items():
+        ms = v.get("kernel_ms", v.get("ms", v.get("ms_per_step")))
+        out["kernels"][k] = [r4(ms), r4(v.get("frac"))] if "frac" in v else r4(ms)
+    err = res.get("errors_vs_fp64") or {}
+    out["errors_vs_fp64"] = {k: [r4(v["max_abs"]), r4(v["rel_l2"])] for k, v in err.items() if isinstance(v, dict)}
+    out["roofline_frac"] = r4((res.get("roofline") or {}).get("frac"))
+    ts = res.get("timestep_2048")
+    if ts:
+        out["timestep_2048"] = {"ms_per_step": r4(ts["ms_per_step"]), "steps": ts["steps"],
+                                "drift": {k: r4(v) for k, v in ts["energy_drift_at_steps"].items()}}
+    en = res.get("ensemble")
+    if en:
+        out["ensemble_ms_per_step"] = r4(en["ms_per_step"])
+    gs = res.get("gs_warm_start")
+    if gs:
+        out["gs"] = {k: r4(gs[k]) for k in ("speedup_learned_vs_plain", "speedup_extrapolated_vs_plain",
+                                              "speedup_net_vs_extrapolated")}
+    cv = res.get("conv_kernels")
+    if cv:
+        out["conv_frac_of_bf16"] = {k: r4(cv[k]["frac_of_bf16_peak"]) for k in ("conv_fwd", "conv_dgrad", "conv_wgrad")}
+    return out
+
+
 def sorted_order(p):
     key = np.floor(p["y"]).astype(np.int64) * NX + np.floor(p["x"]).astype(np.int64)
     return np.argsort(key, kind="stable")
@@ -395,7 +464,9 @@ def run_gpu(args, d: Dist):
     assert ctx.is_sorted()
     q_uniform = ctx.charge_uniform() != 0.0
 
-    # per-scheme sorted kernels
+    peak, peak_kind = peaks()
+    # per-scheme sorted kernels; each scheme's rho is kept for the error report
+    gpu_out = {}
     for nm, s in SCHEMES.items():
         for _ in range(3):
             ctx.deposit(s, ESK_DT, download=False)
@@ -405,10 +476,13 @@ def run_gpu(args, d: Dist):
         ms, cnt = ctx.profile_read("deposit")
         bpp = (BYTES_PER_PARTICLE_ESK if s == 3 else BYTES_PER_PARTICLE) - (BYTES_Q if q_uniform else 0)
         kms = ms / cnt
-        extras[f"{nm}_sorted"] = {"particles_per_s": n / (kms / 1e3), "kernel_ms": kms,
-                                  "kernel_gbs": (bpp * n + BYTES_PER_CELL * G) / (kms / 1e3) / 1e9}
+        gbs = (bpp * n + BYTES_PER_CELL * G) / (kms / 1e3) / 1e9
+        extras[f"{nm}_sorted"] = {"particles_per_s": n / (kms / 1e3), "kernel_ms": kms, "kernel_gbs": gbs,
+                                  "frac": gbs / peak, "bytes_per_particle": bpp}
+        gpu_out[nm] = ctx.deposit(s, ESK_DT)
+    sort_gbs = (48 * n + 4 * (G + 1)) / (sort_ms / 1e3) / 1e9
     extras["sort_random_to_cells"] = {"ms": sort_ms, "particles_per_s": n / (sort_ms / 1e3),
-                                      "algorithmic_gbs": (48 * n + 4 * (G + 1)) / (sort_ms / 1e3) / 1e9}
+                                      "algorithmic_gbs": sort_gbs, "frac": sort_gbs / peak}
     # Esirkepov current of the sorted particles (24 B/particle + 2 x 8 B/cell)
     for _ in range(2):
         ctx.deposit_current(ESK_DT, download=False)
@@ -417,7 +491,9 @@ def run_gpu(args, d: Dist):
         ctx.deposit_current(ESK_DT, download=False)
     ms, cnt = ctx.profile_read("current")
     extras["Esirkepov_current_sorted"] = {"particles_per_s": n / (ms / cnt / 1e3), "kernel_ms": ms / cnt,
-                                          "kernel_gbs": (24 * n + 16 * G) / (ms / cnt / 1e3) / 1e9}
+                                          "kernel_gbs": (24 * n + 16 * G) / (ms / cnt / 1e3) / 1e9,
+                                          "frac": (24 * n + 16 * G) / (ms / cnt / 1e3) / 1e9 / peak}
+    gpu_out["Jx"], gpu_out["Jy"] = ctx.deposit_current(ESK_DT)
     # FFT Poisson on the 1024^2 grid (cuFFT D2Z + k-divide + Z2D), neutral rho
     ctx.deposit(SCHEMES["CIC"], ESK_DT, background=float(PPC), download=False)
     for _ in range(2):
@@ -436,8 +512,9 @@ def run_gpu(args, d: Dist):
     ms, cnt = ctx.profile_read("gather_push")
     # reads cell, xr, yr, vx, vy (+ q when charges differ), writes cell, xr, yr, vx, vy; FP32 Ex, Ey
     gp_bpp = 40 + (0 if q_uniform else 4)
-    extras["gather_push"] = {"particles_per_s": n / (ms / cnt / 1e3), "kernel_ms": ms / cnt,
-                             "kernel_gbs": (gp_bpp * n + 8 * G) / (ms / cnt / 1e3) / 1e9}
+    gp_gbs = (gp_bpp * n + 8 * G) / (ms / cnt / 1e3) / 1e9
+    extras["gather_push"] = {"particles_per_s": n / (ms / cnt / 1e3), "kernel_ms": ms / cnt, "kernel_gbs": gp_gbs,
+                             "frac": gp_gbs / peak}
     # full time step: push, [sort every 10], TSC deposit + background, FFT Poisson,
     # gather, FP64 diagnostics; CUDA-graph replay; host wall time per step
     ctx.run(3, scheme=SCHEMES["TSC"], dt=ESK_DT, background=float(PPC), sort_interval=10, use_graph=True)
@@ -445,6 +522,19 @@ def run_gpu(args, d: Dist):
     ctx.run(20, scheme=SCHEMES["TSC"], dt=ESK_DT, background=float(PPC), sort_interval=10, use_graph=True)
     extras["timestep_tsc_sort10"] = {"ms_per_step": (time.perf_counter() - t0) * 1e3 / 20,
                                      "particles_per_s": n * 20 / (time.perf_counter() - t0)}
+    # the general path: per-particle charges (alternating +-1) are read as a charge stream
+    ctx.upload(p["x"], p["y"], np.where(np.arange(n) % 2 == 0, 1.0, -1.0), p["vx"], p["vy"], p["m"])
+    ctx.sort()
+    for _ in range(3):
+        ctx.deposit(SCHEMES["CIC"], ESK_DT, download=False)
+    ctx.profile_read("deposit")
+    for _ in range(20):
+        ctx.deposit(SCHEMES["CIC"], ESK_DT, download=False)
+    ms, cnt = ctx.profile_read("deposit")
+    gbs = (BYTES_PER_PARTICLE * n + BYTES_PER_CELL * G) / (ms / cnt / 1e3) / 1e9
+    extras["CIC_sorted_per_particle_charges"] = {"particles_per_s": n / (ms / cnt / 1e3), "kernel_ms": ms / cnt,
+                                                 "kernel_gbs": gbs, "frac": gbs / peak,
+                                                 "bytes_per_particle": BYTES_PER_PARTICLE}
     # restore the benchmark state: the random-order particles, cell-sorted
     ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
     ctx.sort()
@@ -477,7 +567,6 @@ def run_gpu(args, d: Dist):
     kernel_ms = kms_tot / max(kcnt, 1)
     bpp_main = BYTES_PER_PARTICLE - (BYTES_Q if q_uniform else 0)
     alg_bytes = bpp_main * n + BYTES_PER_CELL * G
-    peak, peak_kind = peaks()
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     traffic = traffic_from_profile()
 
@@ -519,6 +608,12 @@ def run_gpu(args, d: Dist):
             cpu["detail"] = cpu_detail(ps, threads)
         except Exception as e:  # noqa: BLE001
             cpu["detail"] = {"error": f"{type(e).__name__}: {e}"}
+        try:  # the same leg's FP64 deposits as the checker of the GPU results
+            errors = fp64_errors(p, gpu_out, threads)
+        except Exception as e:  # noqa: BLE001
+            errors = {"error": f"{type(e).__name__}: {e}"}
+    else:
+        errors = None
     for a in list(pin.values()) + [rho_host]:
         a.free()
     ctx.close()
@@ -535,7 +630,7 @@ def run_gpu(args, d: Dist):
                               f"{bpp_main} B/particle" if q_uniform else f"per-particle charges, {bpp_main} B/particle"),
                    "parallelism": f"replicas{d.ws}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": traffic, "kernel": "deposit_tiled<CIC>",
+                     "peak_source": peak_kind, "traffic": traffic, "kernel": "deposit_cells<CIC>",
                      "kernel_ms": kernel_ms, "algorithmic_bytes_per_launch": alg_bytes},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "particles/s", "h2d_bytes_per_step": 24 * n,
@@ -543,6 +638,7 @@ def run_gpu(args, d: Dist):
         "gpu_launches": launches,
         "clocks": clk,
         "extra": extras,
+        "errors_vs_fp64": errors,
     }
 
 
@@ -697,6 +793,9 @@ def run_gs_study(args):
                    "resid_max": float(st["resid"][:, k].max())}
     out["speedup_learned_vs_plain"] = out[names[0]]["ms_mean"] / out[names[2]]["ms_mean"]
     out["speedup_extrapolated_vs_plain"] = out[names[0]]["ms_mean"] / out[names[1]]["ms_mean"]
+    # what the trained network adds to the same method without it
+    out["speedup_net_vs_extrapolated"] = out[names[1]]["ms_mean"] / out[names[2]]["ms_mean"]
+    out["sweeps_net_vs_extrapolated"] = out[names[1]]["sweeps_mean"] / out[names[2]]["sweeps_mean"]
     out["phi_diff_max"] = float(st["phi_diff"].max())
     return out
 
@@ -719,7 +818,7 @@ def main():
     ap.add_argument("--no-gs", action="store_true", help="skip the Gauss-Seidel warm-start study")
     ap.add_argument("--c3-only", action="store_true", help="only the 2048^2 two-stream time step")
     ap.add_argument("--no-c3", action="store_true", help="skip the 2048^2 two-stream time step")
-    ap.add_argument("--c3-steps", type=int, default=200)
+    ap.add_argument("--c3-steps", type=int, default=2000)
     ap.add_argument("--nn-only", action="store_true", help="only the convolution-kernel throughput")
     ap.add_argument("--nn-batch", type=int, default=8)
     ap.add_argument("--nn-reps", type=int, default=5)
@@ -769,6 +868,8 @@ def main():
     finally:
         d.close()
     if res is not None:
+        if args.impl != "reference":
+            res["summary"] = summary(res)
         print(json.dumps(res), flush=True)
 
 

@@ -269,11 +269,15 @@ int pic_gpu_run(pic_ctx* ctx, const pic_run_config* cfg, int steps, pic_diag* hi
  * fixed device array of PIC_NOALLOC_MAX_CELLS cells (8 MiB) that every GPU
  * loading this library holds until the process exits.
  *  - Grids above PIC_NOALLOC_MAX_CELLS cells are rejected with PIC_ERR_ARG.
- *  - Schemes NGP, CIC and TSC; the result equals pic_gpu_deposit's bit for bit
- *    on the same particles. Particles whose key is not below Nx*Ny are skipped.
- *  - The first call on a device looks up the scratch array's device address
- *    (once per device, with that device current); make that first call before
- *    any stream capture.
+ *  - Schemes NGP, CIC and TSC; max_abs_q must be finite and >= 0 (|qn| <= 1 is
+ *    the caller's contract). The result equals pic_gpu_deposit's bit for bit on
+ *    particles with more than one charge value (with one shared charge,
+ *    pic_gpu_deposit's TSC uses exact integer weights: both within the stated
+ *    1e-5 relative L2 of the FP64 deposit). Particles whose key is not below
+ *    Nx*Ny are skipped.
+ *  - The first call in a CUDA context looks up the scratch array's device
+ *    address in that context (once per context, with it current); make that
+ *    first call before any stream capture.
  *  - All calls share the one scratch array, which keeps the last call's sums;
  *    each call clears the part it uses. Calls whose work overlaps on the GPU
  *    (different streams or host threads) race and corrupt each other.

@@ -28,7 +28,16 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libpicref.so")
-REFERENCE_SRC = "/root/reference"
+
+
+def reference_src() -> str | None:
+    """The reference checkout, or None where it is absent: $PIC_REFERENCE_SRC when
+    set, else the location the build recipe (oracle/Makefile, `make print-ref`) names."""
+    path = os.environ.get("PIC_REFERENCE_SRC")
+    if not path:
+        r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+        path = r.stdout.strip() if r.returncode == 0 else ""
+    return path if path and os.path.isdir(path) else None
 
 NGP, CIC, TSC, ESIRKEPOV = 0, 1, 2, 3
 
@@ -45,10 +54,13 @@ class _Domain(C.Structure):
 def build(ref: bool | None = None) -> None:
     """Compile the port (always) and the reference library (when the reference checkout is present)."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    src = reference_src()
     if ref is None:
-        ref = os.path.isdir(REFERENCE_SRC)
+        ref = src is not None
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_SRC}"], check=True)
+        if src is None:
+            raise RuntimeError("the reference checkout is absent: set PIC_REFERENCE_SRC")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
 
 
 def _c(a, dt):

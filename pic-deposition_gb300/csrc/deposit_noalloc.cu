@@ -11,10 +11,16 @@
 // PIC_NOALLOC_MAX_CELLS grid cells; each GPU that loads the library holds that
 // array (8 MiB) until the process exits.
 //
-// The arithmetic is the one of the unsorted (global-atomic) deposit: the same
-// FP32 stencil frames, the same rounding to int32 units with the same node taking
-// each particle's remainder, and the same FP64 conversion, so the
-// result equals pic_gpu_deposit's bit for bit on the same particles.
+// The arithmetic is the general form of the context deposit: the same FP32
+// stencil frames, the same rounding to int32 units with the same node taking
+// each particle's remainder, and the same FP64 conversion, so the result equals
+// pic_gpu_deposit's bit for bit on particles with more than one charge value.
+// (For a set with one shared charge the context deposit's TSC uses exact
+// integer weights at 2^-15 resolution; both stay within the 1e-5 relative L2
+// bound of the FP64 deposit there.)
+#include <cuda.h>  // driver types only: the two driver calls are resolved at run time
+
+#include <cmath>
 #include <mutex>
 
 #include "pic_internal.cuh"
@@ -25,24 +31,64 @@ namespace noalloc {
 static __device__ __align__(256) unsigned long long g_scratch[PIC_NOALLOC_MAX_CELLS];
 
 constexpr int THREADS = 256;
-constexpr int MAX_DEVICES = 64;
+constexpr int MAX_CONTEXTS = 64;
 
-// Device address of g_scratch per device, looked up once with that device current.
+// A __device__ array's address belongs to a CUDA context, not to a device: a
+// host that makes its own driver context current gets a different address
+// than the device's primary context. The address is therefore looked up once
+// per context (keyed by the context's unique id, which is never reused) with
+// that context current, and kept in a small table.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
 static std::mutex g_mutex;
-static void* g_scratch_addr[MAX_DEVICES] = {};
+static CtxGetCurrentFn g_get_current = nullptr;
+static CtxGetIdFn g_get_id = nullptr;
+static unsigned long long g_ctx_id[MAX_CONTEXTS] = {};
+static void* g_scratch_addr[MAX_CONTEXTS] = {};
+static int g_entries = 0;
 
-static int scratch_for_current_device(void** out) {
-    int dev = 0;
-    PIC_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= MAX_DEVICES) return fail(PIC_ERR_UNSUPPORTED, "pic_gpu_deposit_noalloc: device index too large");
+static int resolve_driver_calls() {
+    if (g_get_current && g_get_id) return PIC_OK;
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = cudaDriverEntryPointSymbolNotFound;
+    PIC_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void**)&g_get_current, 12000, cudaEnableDefault, &q1));
+    PIC_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetId", (void**)&g_get_id, 12000, cudaEnableDefault, &q2));
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !g_get_current || !g_get_id)
+        return fail(PIC_ERR_UNSUPPORTED, "pic_gpu_deposit_noalloc: driver does not provide cuCtxGetCurrent/cuCtxGetId");
+    return PIC_OK;
+}
+
+// The scratch array's device address in the current context.
+static int scratch_for_current_context(void** out) {
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
+    PIC_TRY(resolve_driver_calls());
+    CUcontext ctx = nullptr;
+    if (g_get_current(&ctx) != CUDA_SUCCESS) return fail(PIC_ERR_CUDA, "pic_gpu_deposit_noalloc: cuCtxGetCurrent failed");
+    void* p = nullptr;
+    if (!ctx) {
+        // no context is current yet: this runtime call makes the device's primary context current
         const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)");
-        g_scratch_addr[dev] = p;
+        if (g_get_current(&ctx) != CUDA_SUCCESS || !ctx)
+            return fail(PIC_ERR_CUDA, "pic_gpu_deposit_noalloc: no current CUDA context");
     }
-    *out = g_scratch_addr[dev];
+    unsigned long long id = 0;
+    if (g_get_id(ctx, &id) != CUDA_SUCCESS) return fail(PIC_ERR_CUDA, "pic_gpu_deposit_noalloc: cuCtxGetId failed");
+    for (int i = 0; i < g_entries; ++i)
+        if (g_ctx_id[i] == id) {
+            *out = g_scratch_addr[i];
+            return PIC_OK;
+        }
+    if (!p) {
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)");
+    }
+    if (g_entries < MAX_CONTEXTS) {
+        g_ctx_id[g_entries] = id;
+        g_scratch_addr[g_entries] = p;
+        ++g_entries;
+    }
+    *out = p;
     return PIC_OK;
 }
 
@@ -163,10 +209,11 @@ extern "C" int pic_gpu_deposit_noalloc(const pic_domain* dom, int scheme, const 
     if (!rho) return fail(PIC_ERR_ARG, "pic_gpu_deposit_noalloc: NULL output grid");
     if (n > 0 && (!cell || !xr || !yr || !qn)) return fail(PIC_ERR_ARG, "pic_gpu_deposit_noalloc: NULL particle array");
     if (n > ((size_t)1 << 31) - 1) return fail(PIC_ERR_ARG, "pic_gpu_deposit_noalloc: n above 2^31-1");
-    if (!(max_abs_q >= 0.0f)) return fail(PIC_ERR_ARG, "pic_gpu_deposit_noalloc: max_abs_q must be >= 0");
+    if (!(max_abs_q >= 0.0f) || !std::isfinite(max_abs_q))
+        return fail(PIC_ERR_ARG, "pic_gpu_deposit_noalloc: max_abs_q must be finite and >= 0");
 
     void* scratch = nullptr;
-    PIC_TRY(noalloc::scratch_for_current_device(&scratch));
+    PIC_TRY(noalloc::scratch_for_current_context(&scratch));
     cudaStream_t s = (cudaStream_t)stream;
     unsigned long long* acc = (unsigned long long*)scratch;
     // the scratch keeps the previous call's sums: clear the part this grid uses
@@ -182,9 +229,9 @@ extern "C" int pic_gpu_deposit_noalloc(const pic_domain* dom, int scheme, const 
     a.Ny = dom->Ny;
     a.acc = acc;
     if (n > 0) {
-        int dev = 0, sms = 148;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int dev = 0, sms = 0;
+        PIC_CUDA_TRY(cudaGetDevice(&dev));
+        PIC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         size_t blocks = (n + noalloc::THREADS - 1) / noalloc::THREADS;
         if (blocks > (size_t)sms * 16) blocks = (size_t)sms * 16;
         switch (scheme) {

@@ -34,7 +34,7 @@ def port(oracle_mod):
 @pytest.fixture(scope="session")
 def ref(oracle_mod):
     if not oracle_mod.Ref.available():
-        if os.path.isdir(oracle_mod.REFERENCE_SRC):
+        if oracle_mod.reference_src() is not None:
             oracle_mod.build(ref=True)
         else:
             pytest.skip("reference sources not present here (oracle/_ref unavailable)")

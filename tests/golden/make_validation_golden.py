@@ -1,7 +1,8 @@
 """Copies the reference's archived validation results into a small fixture.
 
-Reads, from the reference checkout (default /root/reference, or the path given as
-the first argument), the CSVs its validation driver writes
+Reads, from the reference checkout (the path given as the first argument, else
+the one oracle.reference_src() finds: $PIC_REFERENCE_SRC or the oracle build
+recipe's), the CSVs its validation driver writes
 (src/main_validation.cpp, src/pic/validation.cpp:474-505):
     data/benchmarks/noise_vs_grid.csv, validation.csv, conservation_study.csv,
     two_stream_validation.csv
@@ -13,7 +14,12 @@ import json
 import os
 import sys
 
-src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "oracle"))
+import oracle  # noqa: E402  (test infrastructure: locates the reference checkout)
+
+src = sys.argv[1] if len(sys.argv) > 1 else oracle.reference_src()
+if not src:
+    sys.exit("the reference checkout is absent: pass its path or set PIC_REFERENCE_SRC")
 bench = os.path.join(src, "data", "benchmarks")
 out = {}
 for name in ("noise_vs_grid", "validation", "conservation_study", "two_stream_validation"):
