@@ -80,6 +80,8 @@ class Port:
                                          _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_particle_cell_index.argtypes = [D, C.c_double, C.c_double]
         L.orc_deposit_ref.argtypes = [D, C.c_int, C.c_size_t, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, _dp]
+        L.orc_deposit_timed.argtypes = [D, C.c_int, C.c_size_t, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
+                                        C.c_int, _dp, C.POINTER(C.c_double)]
         L.orc_stable_cell_sort.argtypes = [D, C.c_size_t, _dp, _dp, _u32p, _u32p, _u32p]
         L.orc_stable_sort_keys.argtypes = [C.c_size_t, C.c_uint32, _u32p, _u32p, _u32p, _u32p]
         L.orc_gather_ref.argtypes = [D, C.c_size_t, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double]
@@ -188,6 +190,20 @@ class Port:
                                       _c(p["q"], np.float64), dt, threads, rho)
         assert rc == 0
         return rho
+
+    def deposit_timed(self, nx, ny, lx, ly, scheme, p, dt=0.0, threads=1, warmups=3, repeats=5):
+        """Mean ms of `repeats` deposits after `warmups` untimed ones, timed inside the
+        library as the reference's depositChargeTimedSoA times its deposits."""
+        n = len(p["x"])
+        vx = p.get("vx", np.zeros(n))
+        vy = p.get("vy", np.zeros(n))
+        rho = np.zeros(nx * ny)
+        ms = C.c_double(0)
+        rc = self.lib.orc_deposit_timed(self.dom(nx, ny, lx, ly), scheme, n, _c(p["x"], np.float64),
+                                        _c(p["y"], np.float64), _c(vx, np.float64), _c(vy, np.float64),
+                                        _c(p["q"], np.float64), dt, threads, warmups, repeats, rho, C.byref(ms))
+        assert rc == 0
+        return ms.value
 
     def stable_cell_sort(self, nx, ny, lx, ly, x, y):
         n = len(x)

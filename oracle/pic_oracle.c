@@ -9,6 +9,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -361,6 +362,26 @@ int orc_deposit_ref(const orc_domain* d, int scheme, size_t n, const double* x, 
 /* GPU sort is stable, so its permutation is pinned by a stable counting    */
 /* sort on the same keys, and the per-cell offsets by histogram + scan.     */
 /* ======================================================================= */
+/* depositChargeTimedSoA's timer (src/deposition/deposition.cpp:257-310): `warmups`
+ * untimed deposits, then `repeats` timed ones (each clears rho and deposits, as
+ * depositKernelSoA does); returns the mean deposit time in ms in *mean_ms. */
+int orc_deposit_timed(const orc_domain* d, int scheme, size_t n, const double* x, const double* y, const double* vx,
+                      const double* vy, const double* q, double esirkepov_dt, int threads, int warmups, int repeats,
+                      double* rho, double* mean_ms) {
+    for (int i = 0; i < warmups; ++i)
+        if (orc_deposit_ref(d, scheme, n, x, y, vx, vy, q, esirkepov_dt, threads, rho) != 0) return -1;
+    double sum = 0.0;
+    for (int i = 0; i < repeats; ++i) {
+        struct timespec a, b;
+        clock_gettime(CLOCK_MONOTONIC, &a);
+        if (orc_deposit_ref(d, scheme, n, x, y, vx, vy, q, esirkepov_dt, threads, rho) != 0) return -1;
+        clock_gettime(CLOCK_MONOTONIC, &b);
+        sum += (double)(b.tv_sec - a.tv_sec) * 1e3 + (double)(b.tv_nsec - a.tv_nsec) * 1e-6;
+    }
+    if (mean_ms) *mean_ms = repeats > 0 ? sum / repeats : 0.0;
+    return 0;
+}
+
 int orc_stable_sort_keys(size_t n, uint32_t nkeys, const uint32_t* keys, uint32_t* keys_sorted, uint32_t* perm,
                          uint32_t* offsets) {
     uint32_t* cursor = (uint32_t*)calloc((size_t)nkeys + 1, sizeof(uint32_t));

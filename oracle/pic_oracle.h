@@ -46,6 +46,9 @@ int orc_init_particles(int kind, const orc_domain* d, size_t n, double p0, doubl
 /* ---- FP64 reference deposits (src/deposition/ngp.cpp, deposition_parallel.cpp) ---- */
 int orc_deposit_ref(const orc_domain* d, int scheme, size_t n, const double* x, const double* y, const double* vx,
                     const double* vy, const double* q, double esirkepov_dt, int threads, double* rho);
+int orc_deposit_timed(const orc_domain* d, int scheme, size_t n, const double* x, const double* y, const double* vx,
+                      const double* vy, const double* q, double esirkepov_dt, int threads, int warmups, int repeats,
+                      double* rho, double* mean_ms);
 
 /* ---- stable cell sort (keys bit-exact with src/sorting/cell_sort.cpp:8-13) ---- */
 int orc_stable_cell_sort(const orc_domain* d, size_t n, const double* x, const double* y, uint32_t* keys_sorted,

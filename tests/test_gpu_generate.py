@@ -7,7 +7,9 @@ of the large configuration at a reduced size.
 * The two-stream set-up (ParticlesSoA::initializeTwoStream conventions: charge
   -1/N, m = 1, background 1/V) advanced with TSC, a cell sort every 10 steps and
   the FFT solve tracks the oracle's FP64 restatement of Simulation::run
-  (src/pic/simulation.cpp:82-131) within 1e-5 in total energy over 200 steps.
+  (src/pic/simulation.cpp:82-131; pinned to the reference's own Simulation::run
+  over 2000 steps in test_oracle.py) within 1e-5 in total energy over all 2000
+  steps of the large configuration, at 64 x 64 cells.
 """
 import numpy as np
 import pytest
@@ -47,7 +49,7 @@ def test_generated_statistics(pg):
 def test_two_stream_tsc_tracks_fp64_oracle(pg, port, oracle_mod):
     nx = ny = 64
     n = nx * ny * 16
-    steps, dt = 200, 0.05
+    steps, dt = 2000, 0.05
     with pg.Context(nx, ny, float(nx), float(ny), n) as c:
         c.generate(n, vth=0.01, v0=0.2, charge=-1.0 / n, mass=1.0, seed=5)
         p = c.download()
@@ -56,6 +58,8 @@ def test_two_stream_tsc_tracks_fp64_oracle(pg, port, oracle_mod):
                                   background=1.0 / (nx * ny))
     rel = np.max(np.abs(got[:, 5] - want[:, 5]) / np.abs(want[:, 5]))
     assert rel <= 1e-5, rel
-    drift_gpu = (got[-1, 5] - got[0, 5]) / abs(got[0, 5])
-    drift_ref = (want[-1, 5] - want[0, 5]) / abs(want[0, 5])
-    assert abs(drift_gpu - drift_ref) <= 1e-5, (drift_gpu, drift_ref)
+    # the energy-drift series at the marks the benchmark reports
+    for k in (0, 500, 1000, 1500, steps - 1):
+        drift_gpu = (got[k, 5] - got[0, 5]) / abs(got[0, 5])
+        drift_ref = (want[k, 5] - want[0, 5]) / abs(want[0, 5])
+        assert abs(drift_gpu - drift_ref) <= 1e-5, (k, drift_gpu, drift_ref)

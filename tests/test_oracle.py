@@ -269,3 +269,68 @@ def test_dominant_frequency_matches_reference(port, ref, oracle_mod):
     p = port.init_particles(1, 64, 64, 1.0, 1.0, 200, p0=0.05, mode=1, seed=42)
     h, _ = oracle_mod.simulate(port, 64, 64, 1.0, 1.0, p, CIC, 0.002, 2048, background=1.0)
     assert oracle_mod.dominant_frequency(h[2048 // 4:, 4], 0.002) == out["omega_measured"]
+
+
+def test_port_deposit_speed_matches_the_reference(port, ref):
+    """The port is the timed CPU baseline on hosts where the reference does not build,
+    so its all-core CIC deposit must run at the reference's speed when both are timed
+    the reference's way (depositChargeTimedSoA: untimed warm-ups, then the timed
+    clear + deposit). Best of three at 4 M and 8 M cell-sorted particles, all cores;
+    the port may not be more than 1.3x slower (timing noise)."""
+    import workloads
+
+    threads = os.cpu_count() or 1
+    base = workloads.density_cos(1024, 1024, 8, 0.01, 0.1, seed=3)
+    key = np.floor(base["y"]).astype(np.int64) * 1024 + np.floor(base["x"]).astype(np.int64)
+    o = np.argsort(key, kind="stable")
+    base = {k: v[o] for k, v in base.items()}
+    for n in (4_000_000, 8_000_000):
+        p = {k: np.ascontiguousarray(v[:n]) for k, v in base.items()}
+        t_port = min(port.deposit_timed(1024, 1024, 1024.0, 1024.0, CIC, p, threads=threads, repeats=3)
+                     for _ in range(3))
+        t_ref = min(ref.deposit_timed(1024, 1024, 1024.0, 1024.0, CIC, p, threads=threads, repeats=3)["deposit_ms"]
+                    for _ in range(3))
+        assert t_port <= 1.3 * t_ref, (n, t_port, t_ref)
+
+
+@pytest.mark.parametrize("n,T,dt", [(1000, 0.25, 0.01), (20000, 1.0, 0.004)])
+def test_esirkepov_j_fp64_continuity(port, ref, n, T, dt):
+    """The FP64 Esirkepov current (the oracle's restatement of Esirkepov, CPC 135
+    (2001) 144; the reference has none) conserves charge against the reference's own
+    CIC deposit: (rho_CIC(x + v dt) - rho_CIC(x)) / dt + div J = 0 to round-off, on
+    the set-up of the reference's moving-charge test (src/main_test.cpp:52-72: a
+    Maxwellian in the unit box, 32 x 32 cells)."""
+    nx = ny = 32
+    p = port.init_particles(0, nx, ny, 1.0, 1.0, n, p0=T, seed=123)
+    moved = dict(p, x=p["x"] + p["vx"] * dt, y=p["y"] + p["vy"] * dt)
+    r0 = ref.deposit(nx, ny, 1.0, 1.0, CIC, p)
+    r1 = ref.deposit(nx, ny, 1.0, 1.0, CIC, moved)
+    jx, jy = port.esirkepov_j_ref(nx, ny, 1.0, 1.0, p, dt)
+    JX, JY = jx.reshape(ny, nx), jy.reshape(ny, nx)
+    dx = dy = 1.0 / nx
+    div = (JX - np.roll(JX, 1, axis=1)) / dx + (JY - np.roll(JY, 1, axis=0)) / dy
+    res = (r1 - r0).reshape(ny, nx) / dt + div
+    scale = np.max(np.abs(r0)) / dt
+    assert np.max(np.abs(res)) <= 1e-12 * scale, np.max(np.abs(res)) / scale
+    assert np.max(np.abs(div)) > 1e-3 * scale  # the current is not trivially zero
+
+
+def test_two_stream_tsc_simulation_matches_reference_2000_steps(port, ref, oracle_mod):
+    """The oracle's FP64 time loop (the checker of the GPU's two-stream TSC run) against
+    the reference's own Simulation::run (src/pic/simulation.cpp:69-145) at the reduced
+    size of the large time-step configuration: 64 x 64 cells, 16 particles per cell,
+    initializeTwoStream (beams +-0.2, perturbation 0.01; charge -1/N, background 1/V),
+    TSC, FFT Poisson, dt 0.05, all 2000 steps. Energies agree to FP64 round-off."""
+    nx = ny = 64
+    n = nx * ny * 16
+    steps, dt = 2000, 0.05
+    p = port.init_particles(3, nx, ny, float(nx), float(ny), n, p0=0.2, p1=0.01, seed=17)
+    h, _ = oracle_mod.simulate(port, nx, ny, float(nx), float(ny), p, TSC, dt, steps, background=1.0 / (nx * ny))
+    r = ref.simulation_run(nx, ny, float(nx), float(ny), dt, steps, TSC, n, seed=17, mode=3, beam_velocity=0.2,
+                           perturbation=0.01)
+    assert np.allclose(h[:, 5], r["total"], rtol=1e-9, atol=0)
+    assert np.allclose(h[:, 3], r["kinetic"], rtol=1e-9, atol=0)
+    assert np.allclose(h[:, 4], r["field"], rtol=1e-6, atol=1e-12 * np.max(np.abs(r["field"])))
+    drift_port = (h[-1, 5] - h[0, 5]) / abs(h[0, 5])
+    drift_ref = (r["total"][-1] - r["total"][0]) / abs(r["total"][0])
+    assert abs(drift_port - drift_ref) <= 1e-9
