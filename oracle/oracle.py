@@ -80,6 +80,7 @@ class Port:
                                          _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_particle_cell_index.argtypes = [D, C.c_double, C.c_double]
         L.orc_deposit_ref.argtypes = [D, C.c_int, C.c_size_t, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, _dp]
+        L.orc_sort_particles_by_cell.argtypes = [D, C.c_size_t, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_deposit_timed.argtypes = [D, C.c_int, C.c_size_t, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
                                         C.c_int, _dp, C.POINTER(C.c_double)]
         L.orc_stable_cell_sort.argtypes = [D, C.c_size_t, _dp, _dp, _u32p, _u32p, _u32p]
@@ -204,6 +205,15 @@ class Port:
                                         _c(p["q"], np.float64), dt, threads, warmups, repeats, rho, C.byref(ms))
         assert rc == 0
         return ms.value
+
+    def sort_by_cell(self, nx, ny, lx, ly, p):
+        """The reference's sortParticlesByCell restated (std::sort of an index array by
+        cell key, then a gather of x, y, vx, vy, q, m): a sorted copy of `p`."""
+        out = {k: _c(p[k], np.float64).copy() for k in ("x", "y", "vx", "vy", "q", "m")}
+        rc = self.lib.orc_sort_particles_by_cell(self.dom(nx, ny, lx, ly), len(out["x"]), out["x"], out["y"],
+                                                 out["vx"], out["vy"], out["q"], out["m"])
+        assert rc == 0
+        return out
 
     def stable_cell_sort(self, nx, ny, lx, ly, x, y):
         n = len(x)

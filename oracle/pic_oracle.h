@@ -53,6 +53,9 @@ int orc_deposit_timed(const orc_domain* d, int scheme, size_t n, const double* x
 /* ---- stable cell sort (keys bit-exact with src/sorting/cell_sort.cpp:8-13) ---- */
 int orc_stable_cell_sort(const orc_domain* d, size_t n, const double* x, const double* y, uint32_t* keys_sorted,
                          uint32_t* perm, uint32_t* offsets);
+/* sortParticlesByCell (src/sorting/cell_sort.cpp:22-46), in place (cell_sort_port.cpp) */
+int orc_sort_particles_by_cell(const orc_domain* d, size_t n, double* x, double* y, double* vx, double* vy,
+                               double* q, double* m);
 int orc_stable_sort_keys(size_t n, uint32_t nkeys, const uint32_t* keys, uint32_t* keys_sorted, uint32_t* perm,
                          uint32_t* offsets);
 
