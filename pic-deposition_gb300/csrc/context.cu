@@ -302,12 +302,18 @@ __global__ void check_uniform_charge(const float* __restrict__ q, size_t n, DevS
     if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(&st->q_mixed, 1u);
 }
 
-// Counts adjacent pairs out of cell order (0 => the upload is already sorted).
+// Counts adjacent pairs out of cell order (0 => the upload is already sorted):
+// per warp by ballot, per block in shared memory, one global atomic per block.
 __global__ void count_order_breaks(const uint32_t* __restrict__ cell, size_t n, DevStats* st) {
+    __shared__ unsigned s_breaks;
+    if (threadIdx.x == 0) s_breaks = 0;
+    __syncthreads();
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
     const bool brk = i < n && cell[i] < cell[i - 1];
     const unsigned b = __ballot_sync(0xffffffffu, brk);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&st->order_breaks, (unsigned)__popc(b));
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&s_breaks, (unsigned)__popc(b));
+    __syncthreads();
+    if (threadIdx.x == 0 && s_breaks) atomicAdd(&st->order_breaks, s_breaks);
 }
 
 }  // namespace picgb

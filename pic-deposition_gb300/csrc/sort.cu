@@ -5,75 +5,100 @@
 // (cell_sort.cpp:8-13) and then gathers the six arrays. Here:
 //   * the key is the stored cell key iy*Nx+ix (computed at upload with the
 //     reference's cellCoords, so keys are identical to particleCellIndex);
-//   * the sort is stable, 8-bit digits, ceil(log2(Nx*Ny)/8) passes over
-//     (key, index) pairs; each pass = per-tile digit histogram, device scan of
-//     the digit-major histogram table, and a scatter that ranks keys stably
-//     inside the tile with warp match/ballot ranks and writes them out through
-//     shared memory in digit runs;
-//   * the payload (offsets, velocities, charge, mass) is gathered once through
-//     the final permutation;
-//   * per-cell offsets[Nx*Ny+1] come from a cell histogram and a scan.
+//   * the sort is stable and least-significant digit first, with digits of up
+//     to 10 bits: ceil(bits/10) passes (two at 1024^2 cells, three at 2048^2). A
+//     pass is a per-tile digit histogram, a device scan of the digit-major
+//     histogram table, and a scatter that ranks the tile's keys stably with
+//     warp match/ballot ranks and moves the keys and the whole payload
+//     (offsets, velocities, charge and mass where stored, and the permutation)
+//     through shared memory to the output in digit runs: every global read
+//     and write is coalesced, and no random gather follows the last pass;
+//   * per-cell offsets[Nx*Ny+1] are written from the sorted keys: where the key
+//     changes between i-1 and i, offsets of the cells in between are i.
+#include <utility>
+
 #include "pic_internal.cuh"
 
 namespace picgb {
 
-constexpr int RS_THREADS = 256;
+constexpr int RS_THREADS = 512;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_ITEMS = 16;                        // per thread
-constexpr int RS_TILE = RS_THREADS * RS_ITEMS;      // 4096 keys per tile
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;      // 8192 keys per tile: a 10-bit digit's run fills a sector
 constexpr int RS_WARP_ITEMS = RS_TILE / RS_WARPS;   // 512 keys per warp
-constexpr int RS_RADIX = 256;
+constexpr int RS_MAX_BITS = 10;                     // widest digit (wider ones spill, one CTA per SM)
+constexpr int RS_MAX_PAYLOAD = 7;                   // xr yr vx vy q m perm
 
+// Digit histogram of one tile. When all 32 keys of a warp instruction share a
+// digit (cell-ordered input) they are counted with one shared atomic.
+template <int BITS>
 __global__ void __launch_bounds__(RS_THREADS) radix_histogram(const uint32_t* __restrict__ keys, size_t n,
                                                               int shift, uint32_t mask, uint32_t* __restrict__ counts,
                                                               unsigned num_tiles) {
-    __shared__ uint32_t hist[RS_WARPS][RS_RADIX];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = threadIdx.x; i < RS_WARPS * RS_RADIX; i += RS_THREADS) (&hist[0][0])[i] = 0;
+    constexpr int RADIX = 1 << BITS;
+    __shared__ uint32_t hist[RADIX];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < RADIX; i += RS_THREADS) hist[i] = 0;
     __syncthreads();
     const size_t base = (size_t)blockIdx.x * RS_TILE + (size_t)warp * RS_WARP_ITEMS;
 #pragma unroll 4
     for (int r = 0; r < RS_WARP_ITEMS / 32; ++r) {
         const size_t i = base + (size_t)r * 32 + lane;
-        if (i < n) atomicAdd(&hist[warp][(keys[i] >> shift) & mask], 1u);
+        const uint32_t d = i < n ? (keys[i] >> shift) & mask : 0xffffffffu;
+        const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
+        if (__all_sync(0xffffffffu, d == d0)) {
+            if (lane == 0 && d0 != 0xffffffffu) atomicAdd(&hist[d0], 32u);
+        } else if (d != 0xffffffffu) {
+            atomicAdd(&hist[d], 1u);
+        }
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) {
-        uint32_t s = 0;
-#pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) s += hist[w][d];
-        counts[(size_t)d * num_tiles + blockIdx.x] = s;
-    }
+    for (int d = threadIdx.x; d < RADIX; d += RS_THREADS) counts[(size_t)d * num_tiles + blockIdx.x] = hist[d];
+}
+
+// The fields moved with the keys by a scatter pass: 32-bit words per particle.
+struct Payload {
+    const uint32_t* src[RS_MAX_PAYLOAD];  // NULL with iota: the field is the particle's input index
+    uint32_t* dst[RS_MAX_PAYLOAD];
+    int count;
+};
+
+// Shared memory of the scatter: per-warp 16-bit digit counters (a warp ranks at
+// most 512 keys), tile digit starts, global digit starts, the tile's keys (then
+// each tile slot's output index) and one staged payload field.
+template <int BITS>
+__host__ __device__ constexpr size_t scatter_smem_bytes() {
+    return (size_t)RS_WARPS * (1 << BITS) * 2 + (2 * (size_t)(1 << BITS) + 2 * (size_t)RS_TILE) * 4;
 }
 
 // Scatter of one radix pass. Tile order = (warp, round, lane) = input order, so
 // ranks built warp by warp and round by round are stable.
-__global__ void __launch_bounds__(RS_THREADS) radix_scatter(const uint32_t* __restrict__ keys_in,
-                                                            const uint32_t* __restrict__ vals_in, int iota_vals,
-                                                            uint32_t* __restrict__ keys_out,
-                                                            uint32_t* __restrict__ vals_out, size_t n, int shift,
-                                                            uint32_t mask, const uint32_t* __restrict__ offsets,
-                                                            unsigned num_tiles) {
-    __shared__ uint32_t wcnt[RS_WARPS][RS_RADIX];
-    __shared__ uint32_t bstart[RS_RADIX];
-    __shared__ uint32_t gstart[RS_RADIX];
-    __shared__ uint32_t skeys[RS_TILE];
-    __shared__ uint32_t svals[RS_TILE];
+template <int BITS>
+__global__ void __launch_bounds__(RS_THREADS, 2) radix_scatter(const uint32_t* __restrict__ keys_in,
+                                                               uint32_t* __restrict__ keys_out, size_t n, int shift,
+                                                               uint32_t mask, const uint32_t* __restrict__ offsets,
+                                                               unsigned num_tiles, Payload pay) {
+    constexpr int RADIX = 1 << BITS;
+    extern __shared__ uint32_t rs_smem[];
+    uint32_t* bstart = rs_smem;                     // [RADIX]
+    uint32_t* gstart = bstart + RADIX;              // [RADIX]
+    uint32_t* skeys = gstart + RADIX;               // [RS_TILE]: keys, then output indices
+    uint32_t* sval = skeys + RS_TILE;               // [RS_TILE]
+    uint16_t* wcnt = reinterpret_cast<uint16_t*>(sval + RS_TILE);  // [RS_WARPS][RADIX]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    for (int i = threadIdx.x; i < RS_WARPS * RS_RADIX; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
-    for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) gstart[d] = offsets[(size_t)d * num_tiles + blockIdx.x];
+    for (int i = threadIdx.x; i < RS_WARPS * RADIX; i += RS_THREADS) wcnt[i] = 0;
+    for (int d = threadIdx.x; d < RADIX; d += RS_THREADS) gstart[d] = offsets[(size_t)d * num_tiles + blockIdx.x];
     __syncthreads();
 
     const size_t tile_base = (size_t)blockIdx.x * RS_TILE;
     const size_t base = tile_base + (size_t)warp * RS_WARP_ITEMS;
-    uint32_t k[RS_ITEMS], v[RS_ITEMS], rank[RS_ITEMS];
+    uint32_t k[RS_ITEMS], rank[RS_ITEMS];
 #pragma unroll
     for (int r = 0; r < RS_ITEMS; ++r) {
         const size_t i = base + (size_t)r * 32 + lane;
         const bool ok = i < n;
         k[r] = ok ? keys_in[i] : 0u;
-        v[r] = ok ? (iota_vals ? (uint32_t)i : vals_in[i]) : 0u;
         // lanes with the same digit form one group; its lowest lane advances the
         // warp's counter for that digit by the group size and broadcasts the old value
         const uint32_t d = ok ? ((k[r] >> shift) & mask) : 0xffffffffu;
@@ -81,36 +106,31 @@ __global__ void __launch_bounds__(RS_THREADS) radix_scatter(const uint32_t* __re
         const int leader = __ffs(peers) - 1;
         uint32_t basev = 0;
         if (ok && lane == leader) {
-            basev = wcnt[warp][d];
-            wcnt[warp][d] = basev + (uint32_t)__popc(peers);
+            basev = wcnt[warp * RADIX + d];
+            wcnt[warp * RADIX + d] = (uint16_t)(basev + (uint32_t)__popc(peers));
         }
         basev = __shfl_sync(0xffffffffu, basev, leader);
         rank[r] = ok ? basev + (uint32_t)__popc(peers & lt_mask) : 0xffffffffu;
         __syncwarp();
     }
     __syncthreads();
-    // per-digit warp prefix and tile-local digit starts
-    if (threadIdx.x < RS_RADIX) {
-        const int d = threadIdx.x;
+    // per-digit warp prefix and the tile's digit totals
+    for (int d = threadIdx.x; d < RADIX; d += RS_THREADS) {
         uint32_t s = 0;
 #pragma unroll
         for (int w = 0; w < RS_WARPS; ++w) {
-            const uint32_t c = wcnt[w][d];
-            wcnt[w][d] = s;
+            const uint32_t c = wcnt[w * RADIX + d];
+            wcnt[w * RADIX + d] = (uint16_t)s;  // a tile holds at most 8192 keys
             s += c;
         }
         bstart[d] = s;  // total for now
     }
     __syncthreads();
     if (threadIdx.x < 32) {
-        // exclusive scan of 256 totals by one warp (8 per lane)
-        uint32_t t[8];
+        // exclusive scan of the RADIX totals by one warp (RADIX/32 per lane)
+        constexpr int PER = RADIX / 32 > 0 ? RADIX / 32 : 1;
         uint32_t s = 0;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            t[j] = bstart[lane * 8 + j];
-            s += t[j];
-        }
+        for (int j = 0; j < PER; ++j) s += lane * PER + j < RADIX ? bstart[lane * PER + j] : 0u;
         uint32_t inc = s;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -118,31 +138,57 @@ __global__ void __launch_bounds__(RS_THREADS) radix_scatter(const uint32_t* __re
             if (lane >= o) inc += y;
         }
         uint32_t run = inc - s;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            bstart[lane * 8 + j] = run;
-            run += t[j];
-        }
+        for (int j = 0; j < PER; ++j)
+            if (lane * PER + j < RADIX) {
+                const uint32_t t = bstart[lane * PER + j];
+                bstart[lane * PER + j] = run;
+                run += t;
+            }
     }
     __syncthreads();
+    // tile slot of every item
 #pragma unroll
     for (int r = 0; r < RS_ITEMS; ++r) {
         if (rank[r] != 0xffffffffu) {
             const uint32_t d = (k[r] >> shift) & mask;
-            const uint32_t lp = bstart[d] + wcnt[warp][d] + rank[r];
-            skeys[lp] = k[r];
-            svals[lp] = v[r];
+            rank[r] = bstart[d] + wcnt[warp * RADIX + d] + rank[r];
+            skeys[rank[r]] = k[r];
         }
     }
     __syncthreads();
     const size_t rem = n - tile_base;
     const int tile_n = rem < (size_t)RS_TILE ? (int)rem : RS_TILE;
+    // the first payload field, read in input order while the keys are written out
+    uint32_t pv[RS_ITEMS];
+    auto load_field = [&](int f) {
+        const uint32_t* src = pay.src[f];
+#pragma unroll
+        for (int r = 0; r < RS_ITEMS; ++r) {
+            const size_t i = base + (size_t)r * 32 + lane;
+            pv[r] = rank[r] == 0xffffffffu ? 0u : (src ? src[i] : (uint32_t)i);
+        }
+    };
+    if (pay.count > 0) load_field(0);
+    // tile slot i goes to gstart[d] + (i - bstart[d]): consecutive slots of a digit are
+    // consecutive outputs; each slot's output index replaces its key in skeys
     for (int i = threadIdx.x; i < tile_n; i += RS_THREADS) {
         const uint32_t kk = skeys[i];
         const uint32_t d = (kk >> shift) & mask;
-        const size_t g = (size_t)gstart[d] + (size_t)(i - (int)bstart[d]);
+        const uint32_t g = gstart[d] + (uint32_t)(i - (int)bstart[d]);
         keys_out[g] = kk;
-        vals_out[g] = svals[i];
+        skeys[i] = g;
+    }
+    // the payload, one field at a time through the staging buffer; the next
+    // field's loads are issued before this one is written out
+    for (int f = 0; f < pay.count; ++f) {
+#pragma unroll
+        for (int r = 0; r < RS_ITEMS; ++r)
+            if (rank[r] != 0xffffffffu) sval[rank[r]] = pv[r];
+        __syncthreads();
+        if (f + 1 < pay.count) load_field(f + 1);
+        uint32_t* dst = pay.dst[f];
+        for (int i = threadIdx.x; i < tile_n; i += RS_THREADS) dst[skeys[i]] = sval[i];
+        __syncthreads();
     }
 }
 
@@ -151,21 +197,26 @@ __global__ void iota_u32(uint32_t* __restrict__ out, size_t n) {
     if (i < n) out[i] = (uint32_t)i;
 }
 
-struct GatherArgs {
-    const uint32_t* perm;
-    size_t n;
-    const float* src[6];
-    float* dst[6];
-    int count;
-};
-
-__global__ void gather_payload(GatherArgs a) {
+// offsets[c] = the first index whose key is >= c, from cell-ordered keys: thread
+// i writes i into offsets[keys[i-1]+1 .. keys[i]] (thread 0 from cell 0), the
+// last thread also offsets[keys[n-1]+1 .. G]. Every entry is written once.
+__global__ void offsets_from_sorted(const uint32_t* __restrict__ keys, size_t n, uint32_t G,
+                                    uint32_t* __restrict__ offsets, DevStats* st) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const uint32_t p = a.perm[i];
-#pragma unroll
-    for (int k = 0; k < 6; ++k)
-        if (k < a.count) a.dst[k][i] = __ldg(a.src[k] + p);
+    if (i >= n) return;
+    uint32_t k = keys[i];
+    if (k >= G) {
+        set_dev_error(st, DEV_BAD_CELL, (unsigned int)i);
+        k = G;
+    }
+    uint32_t prev = 0;
+    if (i > 0) {
+        prev = keys[i - 1];
+        prev = prev >= G ? G : prev + 1;
+    }
+    for (uint32_t c = prev; c <= k && c < G; ++c) offsets[c] = (uint32_t)i;
+    if (i + 1 == n)
+        for (uint32_t c = k + 1; c <= G; ++c) offsets[c] = (uint32_t)n;
 }
 
 // Per-cell counts of the sorted keys; runs of equal keys inside a warp are
@@ -203,7 +254,7 @@ int ensure_sort_scratch(pic_ctx* c) {
     if (!c->cellcount) c->cellcount = (uint32_t*)dalloc((c->G + 1) * 4, &rc);
     if (rc) return rc;
     const size_t tiles = (cp + RS_TILE - 1) / RS_TILE;
-    const size_t need = tiles * RS_RADIX;
+    const size_t need = tiles * ((size_t)1 << RS_MAX_BITS);
     if (c->counts_cap < need) {
         dfree(c->counts);
         c->counts = (uint32_t*)dalloc(need * 4, &rc);
@@ -227,6 +278,18 @@ int build_offsets(pic_ctx* c, const uint32_t* keys) {
     return exclusive_scan_u32(c, c->offsets, c->G + 1);
 }
 
+template <int BITS>
+static int launch_pass(pic_ctx* c, const uint32_t* kin, uint32_t* kout, size_t n, int shift, uint32_t mask,
+                       unsigned tiles, const Payload& pay) {
+    radix_histogram<BITS><<<tiles, RS_THREADS, 0, c->stream>>>(kin, n, shift, mask, c->counts, tiles);
+    PIC_TRY(check_launch(c, "radix_histogram"));
+    PIC_TRY(exclusive_scan_u32(c, c->counts, ((size_t)1 << BITS) * tiles));
+    const size_t smem = scatter_smem_bytes<BITS>();
+    PIC_TRY(opt_in_dynamic_smem((const void*)radix_scatter<BITS>, smem));
+    radix_scatter<BITS><<<tiles, RS_THREADS, smem, c->stream>>>(kin, kout, n, shift, mask, c->counts, tiles, pay);
+    return check_launch(c, "radix_scatter");
+}
+
 int sort_particles(pic_ctx* c) {
     PIC_TRY(ensure_sort_scratch(c));
     const size_t n = c->n;
@@ -238,65 +301,48 @@ int sort_particles(pic_ctx* c) {
     const unsigned tiles = (unsigned)((n + RS_TILE - 1) / RS_TILE);
     int bits = 0;
     while (bits < 32 && ((c->G - 1) >> bits) != 0) ++bits;
-    uint32_t* kin = c->cell;
-    uint32_t* kout = c->cell_alt;
-    uint32_t* vin = c->idx_a;
-    uint32_t* vout = c->idx_b;
-    if (bits == 0) {
+    if (bits == 0) {  // one cell: already in order; the permutation is the identity
         iota_u32<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->idx_a, n);
         PIC_TRY(check_launch(c, "iota_u32"));
+        PIC_TRY(build_offsets(c, c->cell));
+        c->sorted = 1;
+        c->part_valid = 1;
+        return PIC_OK;
     }
-    int pass = 0;
-    for (int shift = 0; shift < bits; shift += 8, ++pass) {
-        const int w = (bits - shift) < 8 ? (bits - shift) : 8;
-        const uint32_t mask = (1u << w) - 1u;
-        radix_histogram<<<tiles, RS_THREADS, 0, c->stream>>>(kin, n, shift, mask, c->counts, tiles);
-        PIC_TRY(check_launch(c, "radix_histogram"));
-        PIC_TRY(exclusive_scan_u32(c, c->counts, (size_t)RS_RADIX * tiles));
-        radix_scatter<<<tiles, RS_THREADS, 0, c->stream>>>(kin, vin, pass == 0 ? 1 : 0, kout, vout, n, shift, mask,
-                                                           c->counts, tiles);
-        PIC_TRY(check_launch(c, "radix_scatter"));
-        uint32_t* t = kin;
-        kin = kout;
-        kout = t;
-        t = vin;
-        vin = vout;
-        vout = t;
-    }
-    // kin = sorted keys, vin = permutation
-    if (kin != c->cell) {
-        uint32_t* t = c->cell;
-        c->cell = kin;
-        c->cell_alt = t;
-    }
-    if (vin != c->idx_a) {
-        uint32_t* t = c->idx_a;
-        c->idx_a = vin;
-        c->idx_b = t;
-    }
-    GatherArgs g;
-    g.perm = c->idx_a;
-    g.n = n;
+    const int passes = (bits + RS_MAX_BITS - 1) / RS_MAX_BITS;
+    const int width = (bits + passes - 1) / passes;
     // the payload: offsets, velocities, charges (not when uniform: any order of
-    // equal values is the same array) and masses (when stored)
+    // equal values is the same array), masses (when stored) and the permutation
     float** slots[6] = {&c->xr, &c->yr, &c->vx, &c->vy, &c->q, &c->m};
     int fields[6], nf = 0;
     for (int k = 0; k < 6; ++k)
         if ((k != 4 || c->qn_uniform == 0.0f) && (k != 5 || c->has_mass)) fields[nf++] = k;
-    g.count = nf;
-    for (int j = 0; j < nf; ++j) {
-        g.src[j] = *slots[fields[j]];
-        g.dst[j] = c->alt[fields[j]];
+    for (int pass = 0, shift = 0; pass < passes; ++pass, shift += width) {
+        const int w = (bits - shift) < width ? (bits - shift) : width;
+        const uint32_t mask = (1u << w) - 1u;
+        Payload pay;
+        pay.count = nf + 1;
+        for (int j = 0; j < nf; ++j) {
+            pay.src[j] = reinterpret_cast<const uint32_t*>(*slots[fields[j]]);
+            pay.dst[j] = reinterpret_cast<uint32_t*>(c->alt[fields[j]]);
+        }
+        pay.src[nf] = pass == 0 ? nullptr : c->idx_a;  // the first pass starts from the identity
+        pay.dst[nf] = c->idx_b;
+        int rc;
+        if (width <= 8)
+            rc = launch_pass<8>(c, c->cell, c->cell_alt, n, shift, mask, tiles, pay);
+        else if (width <= 9)
+            rc = launch_pass<9>(c, c->cell, c->cell_alt, n, shift, mask, tiles, pay);
+        else
+            rc = launch_pass<10>(c, c->cell, c->cell_alt, n, shift, mask, tiles, pay);
+        PIC_TRY(rc);
+        std::swap(c->cell, c->cell_alt);
+        std::swap(c->idx_a, c->idx_b);
+        for (int j = 0; j < nf; ++j) std::swap(*slots[fields[j]], c->alt[fields[j]]);
     }
-    gather_payload<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(g);
-    PIC_TRY(check_launch(c, "gather_payload"));
-    for (int j = 0; j < nf; ++j) {
-        const int k = fields[j];
-        float* t = *slots[k];
-        *slots[k] = c->alt[k];
-        c->alt[k] = t;
-    }
-    PIC_TRY(build_offsets(c, c->cell));
+    offsets_from_sorted<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->cell, n, (uint32_t)c->G, c->offsets,
+                                                                             c->dstats);
+    PIC_TRY(check_launch(c, "offsets_from_sorted"));
     c->sorted = 1;
     c->part_valid = 1;
     return PIC_OK;
