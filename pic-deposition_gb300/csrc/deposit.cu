@@ -962,8 +962,10 @@ __global__ void __launch_bounds__(DEP_THREADS, 4) deposit_runs_tsc(DepArgs a) {
 //  * A lane's particles all belong to its cell, so there are no runs to detect
 //    and no cell keys to read: the offsets name every particle's cell (KEYS =
 //    false, a fresh sort). After particles have moved since the sort (KEYS =
-//    true) the keys are read, and a particle that left its cell goes straight
-//    to the global grid.
+//    true, between the sorts of a time-stepping loop) the keys are read;
+//    particles that left their cell are queued per warp (ballot compaction
+//    into shared memory) and, after the stage, all lanes deposit them straight
+//    to the global grid, one per lane (no divergent per-particle path).
 //  * Sums: per stage in 32 bits (at most LPP particles), added to 64-bit cell
 //    totals at the end of each stage (CellRun); the exact integer TSC form
 //    keeps 9 of its 16 entries and 6 axis sums (see CellRun<S_TSC, true>).
@@ -1169,6 +1171,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
     int* shi = reinterpret_cast<int*>(slo + nloc);
     uint32_t* soff = reinterpret_cast<uint32_t*>(shi + nloc);  // the tile rows' offsets, th x (tw + 1)
     const int ow = tw + 1;
+    // KEYS: this warp's queue of particles that left their cell (at most a stage)
+    uint32_t* squeue = soff + a.tile_h * (a.tile_w + 1) + warp * 32 * LPP;
     if (threadIdx.x == 0) s_count = 0;
     for (int i = threadIdx.x; i < nloc; i += NW * 32) {
         slo[i] = 0;
@@ -1271,12 +1275,14 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
         const uint32_t mykey = rowbase + (uint32_t)(x0 + cw.col);
         const unsigned char* sb = swarp + (size_t)buf * BUFB + lane * 16;
         uint32_t scnt = 0;  // particles summed in this stage
+        uint32_t qn = 0;  // particles of this stage that left their cell (KEYS), queued in squeue
 #pragma unroll
         for (int h = 0; h < QL; ++h) {
             const uint32_t qd = cw.q0 + t * QL + (uint32_t)h;
-            if (qd < cw.q1) {
+            const bool qok = qd < cw.q1;
+            if (KEYS || qok) {
                 Quad<S> d;
-                if constexpr (KEYS) d.cell = *reinterpret_cast<const uint4*>(sb + h * 512);
+                if constexpr (KEYS) d.cell = qok ? *reinterpret_cast<const uint4*>(sb + h * 512) : make_uint4(0, 0, 0, 0);
                 d.xr = *reinterpret_cast<const float4*>(sb + (FX * QL + h) * 512);
                 d.yr = *reinterpret_cast<const float4*>(sb + ((FX + 1) * QL + h) * 512);
                 if constexpr (QC)
@@ -1290,18 +1296,23 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const uint32_t p = 4u * qd + (uint32_t)k;
-                    if (p - cw.beg < cw.end - cw.beg) {
+                    bool valid = qok && p - cw.beg < cw.end - cw.beg;
+                    if constexpr (KEYS) {
+                        // a particle that left its cell since the last sort is queued and
+                        // deposited after the stage by all lanes together (no divergent path)
+                        const bool stale = valid && u4(d.cell, k) != mykey;
+                        const unsigned sb_mask = __ballot_sync(FULL, stale);
+                        if (sb_mask) {
+                            if (stale) squeue[qn + __popc(sb_mask & ((1u << lane) - 1u))] = p;
+                            qn += __popc(sb_mask);
+                            valid = valid && !stale;
+                        }
+                    }
+                    if (valid) {
                         float vxx = 0.0f, vyy = 0.0f;
                         if constexpr (S == S_ESK) {
                             vxx = f4(d.vx, k);
                             vyy = f4(d.vy, k);
-                        }
-                        if constexpr (KEYS) {
-                            const uint32_t key = u4(d.cell, k);
-                            if (key != mykey) {  // left its cell since the last sort
-                                stale_to_global<S, QC>(a, key, f4(d.xr, k), f4(d.yr, k), f4(d.q, k), vxx, vyy, p);
-                                continue;
-                            }
                         }
                         if constexpr (TSCI || (S == S_NGP && QC)) {
                             run.add(f4(d.xr, k), f4(d.yr, k));
@@ -1319,6 +1330,21 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
                     }
                 }
                 run.end_quad();
+            }
+        }
+        if constexpr (KEYS) {
+            if (qn) {  // the stage's particles that left their cell, one per lane
+                __syncwarp();
+                for (uint32_t i = (uint32_t)lane; i < qn; i += 32) {
+                    const uint32_t p = squeue[i];
+                    float vxx = 0.0f, vyy = 0.0f;
+                    if constexpr (S == S_ESK) {
+                        vxx = a.vx[p];
+                        vyy = a.vy[p];
+                    }
+                    stale_to_global<S, QC>(a, a.cell[p], a.xr[p], a.yr[p], QC ? a.qc : a.q[p], vxx, vyy, p);
+                }
+                __syncwarp();
             }
         }
         run.end_stage(scnt, (t + 1u) % FOLD == 0u);
@@ -1387,6 +1413,7 @@ __global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double
 #ifndef CELLS_LPP
 #define CELLS_LPP 8
 #endif
+
 #ifndef CELLS_NBUF
 #define CELLS_NBUF 2
 #endif
@@ -1395,7 +1422,8 @@ static int launch_cells(pic_ctx* c, const DepArgs& a, unsigned tiles) {
     constexpr int NBUF = CELLS_NBUF;
     const size_t smem = cells_fixed_bytes<S, LPP, NW, QC, KEYS, NBUF>() +
                         (size_t)(a.tile_h + 3) * (a.tile_w + 3) * 2 * sizeof(uint32_t) +
-                        (size_t)a.tile_h * (a.tile_w + 1) * sizeof(uint32_t);
+                        (size_t)a.tile_h * (a.tile_w + 1) * sizeof(uint32_t) +
+                        (KEYS ? (size_t)NW * 32 * LPP * sizeof(uint32_t) : 0);
     const int rc = opt_in_dynamic_smem((const void*)deposit_cells<S, LPP, NW, MINB, QC, KEYS, NBUF>, smem);
     if (rc != PIC_OK) return rc;
     deposit_cells<S, LPP, NW, MINB, QC, KEYS, NBUF><<<tiles, NW * 32, smem, c->stream>>>(a);
@@ -1466,9 +1494,10 @@ int deposit_rho(pic_ctx* c, int scheme, double dt, double background) {
     } else if (c->order_mode == PIC_ORDER_ATOMIC) {
         tiled = 2;
     } else {
-        // between sorts the run-aggregating kernel: particles of neighbouring
-        // cells interleave within a cell's range and break the lanes' runs
-        tiled = c->sorted ? 0 : 1;
+        // between sorts (the last sort's cell ranges still index the particles) the
+        // cell kernel walks those ranges and deposits the particles that moved to
+        // another cell on their own; otherwise the run-aggregating kernel
+        tiled = (c->sorted || c->part_valid) ? 0 : 1;
     }
     PIC_CUDA_TRY(cudaMemsetAsync(c->acc, 0, c->G * sizeof(long long), c->stream));
     DepArgs a;
