@@ -256,6 +256,26 @@ def run_deposit_only(args, d: Dist):
                       "mean_kernel_ms": ms / cnt}))
 
 
+def run_sort_only(args, d: Dist):
+    """Reduced run for profilers: warmup + steps cell sorts of the workload, each of the
+    random-order (generation-order) upload; prints the mean sort time."""
+    import pic_gb300 as pg
+
+    p = make_workload(42)
+    n = len(p["x"])
+    with pg.Context(NX, NY, float(NX), float(NY), n) as ctx:
+        ctx.profile(True)
+        ms = []
+        for i in range(args.warmup + args.steps):
+            ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+            ctx.profile_read("sort")
+            ctx.sort()
+            t, cnt = ctx.profile_read("sort")
+            if i >= args.warmup:
+                ms.append(t / cnt)
+    print(json.dumps({"sort_only": "random order", "particles": n, "grid": [NX, NY], "mean_sort_ms": sum(ms) / len(ms)}))
+
+
 def cpu_deposit_timer(threads: int):
     """Returns (fn(p) -> seconds for one FP64 CIC deposit, kind)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -815,6 +835,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ppc", type=int, default=PPC, help="particles per cell (64 = the benchmark workload)")
     ap.add_argument("--deposit-only", action="store_true", help="reduced run for profilers")
+    ap.add_argument("--sort-only", action="store_true", help="reduced run for profilers: cell sorts only")
     ap.add_argument("--order", default="sorted", choices=["sorted", "random"],
                     help="--deposit-only: cell-sorted particles or the generation order")
     ap.add_argument("--gs-only", action="store_true", help="only the Gauss-Seidel warm-start study")
@@ -856,6 +877,10 @@ def main():
     d = Dist()
     if args.deposit_only:
         run_deposit_only(args, d)
+        d.close()
+        return
+    if args.sort_only:
+        run_sort_only(args, d)
         d.close()
         return
     try:
