@@ -674,29 +674,46 @@ def ensemble_members(seed=4, runs=64):
     return [(int(n), int(p), int(1000 + i)) for i, (n, p) in enumerate(zip(ns, ppcs))]
 
 
-def run_ensemble(args):
+def run_ensemble(args, d=None):
     """Batched ensemble: every run's step (gather+push, deposit, FFT Poisson) in one
-    persistent launch + batched FFTs per step, replayed as a CUDA graph."""
+    persistent launch + batched FFTs per step, replayed as a CUDA graph. Over N
+    ranks each rank runs its share of the members (partition_members, balanced
+    by particles) as its own batch; the step time is the max over ranks and the
+    throughput counts every member (strong scaling: the members are fixed)."""
     import pic_gb300 as pg
 
     members = ensemble_members(runs=args.ens_runs)
+    ws, rank = (d.ws, d.rank) if d is not None else (1, 0)
+    mine = pg.partition_members(members, ws)[rank]
     total = sum(n * n * p for n, p, _ in members)
     out = {"workload": f"ensemble_{len(members)}_langmuir_runs", "runs": len(members), "particles": total,
            "cells": sum(n * n for n, _, _ in members), "dt": 0.1, "amplitude": 0.01, "vth": 0.05,
-           "sort_interval": args.ens_sort, "steps": args.ens_steps}
-    with pg.Ensemble(members, dt=0.1, amplitude=0.01, vth=0.05, sort_interval=args.ens_sort, use_graph=True) as e:
-        e.run(args.ens_sort + 1)  # warm-up: first sort, autotuning, graph capture
-        stream = e.stream()
-        ev = CudaEvents()
-        e0, e1 = ev.event(), ev.event()
-        l0 = e.launch_count()
-        ev.record(e0, stream)
-        fe, ke = e.run(args.ens_steps)
-        ev.record(e1, stream)
-        ms = ev.elapsed_ms(e0, e1)
-        out["launches_per_step"] = (e.launch_count() - l0) / args.ens_steps
-        out["tiles"] = sorted({f"N{e.info(r)['N']}_ppc{e.info(r)['ppc']}": list(e.info(r)["tile"])
-                               for r in range(len(members))}.items())
+           "sort_interval": args.ens_sort, "steps": args.ens_steps, "ranks": ws,
+           "scaling": "strong" if ws > 1 else None}
+    ms, fe = 0.0, np.zeros((1, 0))
+    if d is not None:
+        d.barrier()
+    if mine:
+        with pg.Ensemble([members[i] for i in mine], dt=0.1, amplitude=0.01, vth=0.05, sort_interval=args.ens_sort,
+                         use_graph=True, device=d.local if d is not None else 0) as e:
+            e.run(args.ens_sort + 1)  # warm-up: first sort, autotuning, graph capture
+            stream = e.stream()
+            ev = CudaEvents()
+            e0, e1 = ev.event(), ev.event()
+            l0 = e.launch_count()
+            if d is not None:
+                d.barrier()
+            ev.record(e0, stream)
+            fe, ke = e.run(args.ens_steps)
+            ev.record(e1, stream)
+            ms = ev.elapsed_ms(e0, e1)
+            out["launches_per_step"] = (e.launch_count() - l0) / args.ens_steps
+            out["tiles"] = sorted({f"N{e.info(r)['N']}_ppc{e.info(r)['ppc']}": list(e.info(r)["tile"])
+                                   for r in range(len(mine))}.items())
+    elif d is not None:
+        d.barrier()
+    if d is not None:
+        ms = d.max(ms)
     out["ms_per_step"] = ms / args.ens_steps
     out["particle_steps_per_s"] = total * args.ens_steps / (ms * 1e-3)
     out["field_energy_finite"] = bool(np.all(np.isfinite(fe)))
@@ -866,7 +883,13 @@ def main():
         print(json.dumps(run_gs_study(args)), flush=True)
         return
     if args.ens_only:
-        print(json.dumps(run_ensemble(args)), flush=True)
+        d = Dist()
+        try:
+            res = run_ensemble(args, d)
+        finally:
+            d.close()
+        if d.rank == 0:
+            print(json.dumps(res), flush=True)
         return
     if args.nn_only:
         print(json.dumps(run_nn_profile(args)), flush=True)

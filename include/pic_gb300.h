@@ -222,6 +222,15 @@ int pic_gpu_poisson_rbgs(pic_ctx* ctx, double tol, int max_iters, int warm_start
  * grid that tiles into 64x32 (or smaller power-of-two) tiles, else it runs mode 0. */
 int pic_gpu_set_rbgs_precision(pic_ctx* ctx, int mixed);
 
+/* Test hook of the bounded device waits (no counterpart in the reference): runs
+ * the one-launch FP64 red-black solve on the context's rho (phi from 0, 64
+ * sweeps) with CTA absent_block leaving before its first grid barrier (-1: none)
+ * and every barrier wait limited to wait_ms (0 < wait_ms <= 1000). The other
+ * CTAs give up, set the error flag and return; the call returns PIC_ERR_TIMEOUT
+ * and the context stays usable. PIC_ERR_UNSUPPORTED when the grid does not fit
+ * one cooperative launch. */
+int pic_gpu_test_rbgs_barrier_timeout(pic_ctx* ctx, int absent_block, double wait_ms);
+
 /* ---- particle motion ---- */
 
 /* pic::gatherFieldsSoA (src/deposition/deposition.cpp:335-356): v += -(q/m)*E*dt. */
@@ -354,7 +363,9 @@ typedef struct pic_ens pic_ens;
 typedef struct pic_ens_member {
     int N;          /* grid N x N (even) */
     int ppc;        /* particles per cell */
-    unsigned seed;  /* per-run seed (mixed with pic_ens_config.seed) */
+    unsigned seed;  /* per-run seed (mixed with pic_ens_config.seed); a run's initial state
+                     * depends on its N, ppc, seed and the config only, not on the other
+                     * runs of the batch, so a batch can be split over GPUs */
 } pic_ens_member;
 typedef struct pic_ens_config {
     double dt;

@@ -429,6 +429,7 @@ struct InitArgs {
     const RunDesc* runs;
     int run;
     uint32_t seed;
+    uint32_t member_seed;  // the member's own seed: its stream does not depend on its place in the batch
     double amp, vth;
     uint32_t* cell;
     float *xr, *yr, *vx, *vy, *q;
@@ -444,7 +445,7 @@ __global__ void ens_init_run(InitArgs a) {
     U4 c;
     c.v[0] = (uint32_t)i;
     c.v[1] = (uint32_t)((uint64_t)i >> 32);
-    c.v[2] = (uint32_t)a.run;
+    c.v[2] = a.member_seed;
     c.v[3] = 0x5EED0001u;
     const U4 u = philox(c, a.seed, 0x7A3C91E5u);
     c.v[3] = 0x5EED0002u;
@@ -970,8 +971,8 @@ int pic_ens_create(const pic_ens_member* runs_in, int nruns, const pic_ens_confi
         out_rc = fail(PIC_ERR_CUDA, "ensemble setup copy");
     // particles
     for (int i = 0; i < nruns && out_rc == PIC_OK; ++i) {
-        InitArgs ia{e->druns, i, cfg->seed ^ (uint32_t)(runs_in[order[i]].seed * 2654435761u), e->amp, e->vth,
-                    c->cell, c->xr, c->yr, c->vx, c->vy, c->q};
+        InitArgs ia{e->druns, i, cfg->seed ^ (uint32_t)(runs_in[order[i]].seed * 2654435761u),
+                    runs_in[order[i]].seed, e->amp, e->vth, c->cell, c->xr, c->yr, c->vx, c->vy, c->q};
         const size_t np = e->runs[i].np;
         ens_init_run<<<(unsigned)((np + 255) / 256), 256, 0, c->stream>>>(ia);
         out_rc = check_launch(c, "ens_init_run");

@@ -200,6 +200,7 @@ static int rb_finish(pic_ctx* c) {
 constexpr int PS_THREADS = RB_THREADS;
 constexpr int PS_HALO = 4;
 constexpr int PS_MAX_BLOCKS = 4096;
+constexpr unsigned long long PS_WAIT_NS = 1000000000ull;
 
 struct PsArgs {
     RbArgs a;
@@ -210,6 +211,8 @@ struct PsArgs {
     unsigned* bar;    // [0] arrivals, [1] generation
     int* err;
     double* out;      // [0] sweeps, [1] residual, [2] first residual
+    int absent_block; // -1, or a CTA that leaves at once (the timeout test hook)
+    unsigned long long wait_ns;  // limit of one barrier wait
 };
 
 __device__ __forceinline__ uint64_t ps_time_ns() {
@@ -218,7 +221,7 @@ __device__ __forceinline__ uint64_t ps_time_ns() {
     return t;
 }
 
-__device__ bool ps_barrier(unsigned* bar, int* err) {
+__device__ bool ps_barrier(unsigned* bar, int* err, unsigned long long wait_ns = PS_WAIT_NS) {
     __syncthreads();
     __shared__ int ok;
     if (threadIdx.x == 0) {
@@ -233,7 +236,7 @@ __device__ bool ps_barrier(unsigned* bar, int* err) {
         } else {
             const uint64_t t0 = ps_time_ns();
             while (*vgen == gen)
-                if (ps_time_ns() - t0 > 1000000000ull) {
+                if (ps_time_ns() - t0 > wait_ns) {
                     atomicExch(err, 1);
                     ok = 0;
                     break;
@@ -257,6 +260,7 @@ __global__ void __launch_bounds__(PS_THREADS) rbgs_persistent(PsArgs p) {
     double* sb = psm + E;
     __shared__ double tot[2];
     const RbArgs& a = p.a;
+    if ((int)blockIdx.x == p.absent_block) return;
     const int tx = blockIdx.x % p.tiles_x, ty = blockIdx.x / p.tiles_x;
     const int ox = tx * p.tw - PS_HALO, oy = ty * p.th - PS_HALO;
     for (int i = threadIdx.x; i < E; i += PS_THREADS) {
@@ -290,7 +294,7 @@ __global__ void __launch_bounds__(PS_THREADS) rbgs_persistent(PsArgs p) {
             }
             rr = rb_block_sum(rr);
             if (threadIdx.x == 0) p.partial[2 * blockIdx.x] = rr;
-            if (!ps_barrier(p.bar, p.err)) break;
+            if (!ps_barrier(p.bar, p.err, p.wait_ns)) break;
             if (threadIdx.x == 0) {
                 double s1 = 0.0, s2 = 0.0;
                 for (unsigned k = 0; k < gridDim.x; ++k) {
@@ -328,7 +332,7 @@ __global__ void __launch_bounds__(PS_THREADS) rbgs_persistent(PsArgs p) {
             const int ly = PS_HALO + t / p.tw, lx = PS_HALO + t % p.tw;
             a.phi[(size_t)(oy + ly) * a.Nx + (ox + lx)] = sphi[ly * p.ew + lx];
         }
-        if (!ps_barrier(p.bar, p.err)) break;
+        if (!ps_barrier(p.bar, p.err, p.wait_ns)) break;
         for (int i = threadIdx.x; i < E; i += PS_THREADS) {
             const int ly = i / p.ew, lx = i - ly * p.ew;
             if (ly >= PS_HALO && ly < PS_HALO + p.th && lx >= PS_HALO && lx < PS_HALO + p.tw) continue;
@@ -351,8 +355,10 @@ static int largest_divisor_tile(int n, const int* cand, int ncand) {
 
 // Solves in one cooperative launch when the grid tiles evenly and every CTA can
 // be resident; returns PIC_ERR_UNSUPPORTED (nothing queued) otherwise.
+// absent_block >= 0 makes that CTA leave before its first barrier, so that every
+// other CTA's wait runs out after wait_ns (the timeout test hook; -1 in solves).
 static int rbgs_solve_persistent(pic_ctx* c, const RbArgs& a, double tol, int max_iters, int check_every, int* it,
-                                 double* res) {
+                                 double* res, int absent_block = -1, unsigned long long wait_ns = PS_WAIT_NS) {
     if ((check_every & 1) || (max_iters & 1)) return PIC_ERR_UNSUPPORTED;
     static const int cw[] = {64, 32, 16, 8, 4, 2};
     static const int ch[] = {32, 16, 8, 4, 2};
@@ -376,7 +382,8 @@ static int rbgs_solve_persistent(pic_ctx* c, const RbArgs& a, double tol, int ma
     int* err = reinterpret_cast<int*>(out + 5);
     PIC_CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), c->stream));
     PIC_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-    PsArgs p{a, tw, th, tiles_x, ew, eh, tol, max_iters, check_every, c->rb_ps, bar, err, out};
+    PsArgs p{a,   tw,  th,  tiles_x, ew,  eh,           tol,    max_iters,
+             check_every, c->rb_ps, bar, err,     out, absent_block, wait_ns};
     cudaLaunchConfig_t lc{};
     lc.gridDim = dim3(blocks);
     lc.blockDim = dim3(PS_THREADS);
@@ -635,7 +642,10 @@ int rbgs_solve(pic_ctx* c, double tol, int max_iters, int check_every, int* iter
     if (c->rbgs_mixed) prc = rbgs_solve_mixed(c, a, tol, max_iters, check_every, &it, &res);
     if (prc == PIC_ERR_UNSUPPORTED && c->rbgs_persistent)
         prc = rbgs_solve_persistent(c, a, tol, max_iters, check_every, &it, &res);
-    if (prc != PIC_OK && prc != PIC_ERR_UNSUPPORTED) return prc;
+    if (prc != PIC_OK && prc != PIC_ERR_UNSUPPORTED) {
+        prof_end(c);
+        return prc;
+    }
     for (; prc == PIC_ERR_UNSUPPORTED;) {
         PIC_TRY(rb_residual_async(c, a));
         double s[3];
@@ -710,6 +720,29 @@ extern "C" int pic_gpu_set_rbgs_precision(pic_ctx* c, int mixed) {
     if (mixed != 0 && mixed != 1) return fail(PIC_ERR_ARG, "precision must be 0 (FP64) or 1 (mixed)");
     c->rbgs_mixed = mixed;
     return PIC_OK;
+}
+
+// Runs the persistent FP64 solve on the context's rho with CTA `absent_block`
+// leaving at once and every barrier wait limited to wait_ms: the other CTAs give
+// up, set the error flag and return, and the call reports PIC_ERR_TIMEOUT.
+extern "C" int pic_gpu_test_rbgs_barrier_timeout(pic_ctx* c, int absent_block, double wait_ms) {
+    if (!c) return fail(PIC_ERR_ARG, "NULL context");
+    if (absent_block < -1) return fail(PIC_ERR_ARG, "absent_block < -1");
+    if (!(wait_ms > 0.0 && wait_ms <= 1000.0)) return fail(PIC_ERR_ARG, "wait_ms must be in (0, 1000]");
+    if ((c->Nx & 1) || (c->Ny & 1)) return fail(PIC_ERR_UNSUPPORTED, "red-black Gauss-Seidel needs even Nx and Ny");
+    PIC_CUDA_TRY(cudaSetDevice(c->device));
+    PIC_TRY(ensure_fields(c));
+    PIC_TRY(ensure_rbgs(c));
+    PIC_TRY(rb_prepare(c));
+    PIC_CUDA_TRY(cudaMemsetAsync(c->phi, 0, c->G * 8, c->stream));
+    const RbArgs a = rb_args(c);
+    int it = 0;
+    double res = 0.0;
+    const int rc = rbgs_solve_persistent(c, a, 0.0, 64, 2, &it, &res, absent_block,
+                                         (unsigned long long)(wait_ms * 1e6));
+    if (rc == PIC_ERR_UNSUPPORTED) return fail(rc, "the grid does not fit one cooperative launch");
+    if (rc != PIC_OK) return rc;
+    return pic_gpu_synchronize(c);
 }
 
 extern "C" int pic_gpu_poisson_rbgs(pic_ctx* c, double tol, int max_iters, int warm_start, int check_every,

@@ -125,6 +125,67 @@ _SIGS += [
 ]
 
 
+def partition_members(runs, world_size: int):
+    """Ensemble members split over `world_size` ranks, balanced by particle count.
+
+    The reference's multi-seed sweep (src/pic/physics_studies.cpp:479-560) runs
+    its members one after another; here each rank runs a share of them as one
+    batched ensemble on its own GPU. Largest members first, each to the rank with
+    the fewest particles so far (lowest rank on ties). Returns one ascending list
+    of member indices per rank: every member appears exactly once.
+    """
+    if world_size < 1:
+        raise ValueError("world_size must be >= 1")
+    load = [0] * world_size
+    parts = [[] for _ in range(world_size)]
+    sizes = [int(n) * int(n) * int(p) for n, p, _ in runs]
+    for i in sorted(range(len(runs)), key=lambda i: (-sizes[i], i)):
+        r = min(range(world_size), key=lambda k: (load[k], k))
+        parts[r].append(i)
+        load[r] += sizes[i]
+    return [sorted(p) for p in parts]
+
+
+def run_ensemble_ranks(runs, steps: int, rank: int = 0, world_size: int = 1, ensemble=None, **cfg):
+    """This rank's share of an ensemble (partition_members), advanced `steps` steps.
+
+    A member's run depends only on its own (N, ppc, seed) and the shared
+    configuration, so the share runs as its own batched ensemble. The one
+    exchange is a final gather of the per-member energy histories to rank 0
+    (torch.distributed.gather_object on the initialised process group). Returns
+    (field_energy, kinetic_energy), each (steps, len(runs)) in the order of
+    `runs`, on rank 0, and None on the other ranks. `ensemble` builds the
+    batch (default: Ensemble) and takes (members, **cfg).
+    """
+    make = ensemble or Ensemble
+    mine = partition_members(runs, world_size)[rank]
+    fe = ke = np.zeros((steps, 0))
+    if mine:
+        with make([runs[i] for i in mine], **cfg) as e:
+            fe, ke = e.run_member_order(steps)
+    part = (mine, np.asarray(fe), np.asarray(ke))
+    if world_size > 1:
+        import torch.distributed as dist
+
+        got = [None] * world_size if rank == 0 else None
+        dist.gather_object(part, got, dst=0)
+        if rank != 0:
+            return None
+    else:
+        got = [part]
+    out_fe = np.full((steps, len(runs)), np.nan)
+    out_ke = np.full((steps, len(runs)), np.nan)
+    seen = np.zeros(len(runs), np.int64)
+    for idx, f, k in got:
+        for j, i in enumerate(idx):
+            out_fe[:, i] = f[:, j]
+            out_ke[:, i] = k[:, j]
+            seen[i] += 1
+    if not np.all(seen == 1):
+        raise RuntimeError("ensemble ranks: the gathered members do not cover every run exactly once")
+    return out_fe, out_ke
+
+
 def nn_conv3x3(op: int, x: np.ndarray, weight=None, bias=None, aux=None, cin: int = 32, cout: int = 32):
     """One tensor-core convolution layer on host arrays (pic_nn_conv3x3).
 
@@ -165,6 +226,7 @@ class GenConfig(C.Structure):
 
 _SIGS.append(("pic_gpu_generate", [_vp, C.POINTER(GenConfig)]))
 _SIGS.append(("pic_gpu_set_rbgs_precision", [_vp, C.c_int]))
+_SIGS.append(("pic_gpu_test_rbgs_barrier_timeout", [_vp, C.c_int, C.c_double]))
 
 
 class EnsMember(C.Structure):
@@ -205,6 +267,8 @@ class Ensemble:
         _check(lib().pic_ens_create(arr, len(runs), C.byref(cfg), int(device), C.byref(h)))
         self.h = h
         self.nruns = len(runs)
+        # the library's order: a stable sort of the runs by grid size
+        self.order = sorted(range(len(runs)), key=lambda i: int(runs[i][0]))
 
     def close(self):
         if self.h:
@@ -228,6 +292,13 @@ class Ensemble:
         ke = np.zeros((max(steps, 1), self.nruns))
         _check(lib().pic_ens_run(self.h, int(steps), _ptr(fe), _ptr(ke)))
         return fe[:steps], ke[:steps]
+
+    def run_member_order(self, steps):
+        """run(steps) with the columns put back in the order of the `runs` given."""
+        fe, ke = self.run(steps)
+        back = np.empty(self.nruns, np.int64)
+        back[self.order] = np.arange(self.nruns)
+        return fe[:, back], ke[:, back]
 
     def info(self, r):
         i = EnsRunInfo()
@@ -471,6 +542,12 @@ class Context:
     def set_rbgs_precision(self, mixed: bool):
         """False: FP64 sweeps; True: FP32 sweeps on FP64-refined corrections."""
         _check(lib().pic_gpu_set_rbgs_precision(self.h, 1 if mixed else 0))
+
+    def test_rbgs_barrier_timeout(self, absent_block: int, wait_ms: float = 1.0):
+        """Test hook: the one-launch FP64 solve with CTA absent_block (-1: none)
+        leaving before its first grid barrier and each barrier wait limited to
+        wait_ms; raises PicError(PIC_ERR_TIMEOUT) when a wait ran out."""
+        _check(lib().pic_gpu_test_rbgs_barrier_timeout(self.h, int(absent_block), float(wait_ms)))
 
     def poisson_rbgs(self, tol=1e-8, max_iters=1_000_000, warm_start=True, check_every=64):
         it = C.c_int()

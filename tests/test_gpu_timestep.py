@@ -175,6 +175,35 @@ def test_rbgs_mixed_precision_meets_the_same_fp64_test(pg, nx, ny):
     assert np.max(np.abs(p1 - p0)) <= 1e-6 * np.max(np.abs(p0))
 
 
+@pytest.mark.parametrize("absent", [5, 0])
+def test_rbgs_barrier_timeout_reported_and_context_usable(pg, port, absent):
+    """One CTA of the one-launch solve leaves before its first grid barrier:
+    every other CTA's wait runs out after 1 ms and returns, the call reports
+    PIC_ERR_TIMEOUT, and the same context then solves and deposits exactly as a
+    fresh one does."""
+    nx, ny = 512, 512  # 64x32 tiles: 128 CTAs in one cooperative launch
+    rng = np.random.default_rng(5)
+    rho = rng.normal(size=nx * ny)
+    p = port.init_particles(0, nx, ny, 1.0, 1.0, 20000, p0=1.0, seed=9)
+    out = []
+    for fault in (False, True):
+        with pg.Context(nx, ny, 1.0, 1.0, len(p["x"])) as c:
+            c.set_rho(rho)
+            if fault:
+                c.test_rbgs_barrier_timeout(-1, 1.0)  # nobody absent: completes
+                with pytest.raises(pg.PicError) as e:
+                    c.test_rbgs_barrier_timeout(absent, 1.0)
+                assert e.value.code == -7 and "timed out" in str(e.value)
+            it, _ = c.poisson_rbgs(tol=0.0, max_iters=40, warm_start=False, check_every=40)
+            phi = c.fields()[0]
+            c.upload(p["x"], p["y"], p["q"])
+            rho_dep = c.deposit(CIC)
+            out.append((it, phi, rho_dep))
+    assert out[0][0] == out[1][0] == 40
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2])
+
+
 def test_rbgs_odd_grid_rejected(pg):
     with pg.Context(33, 32, 1.0, 1.0, 1) as c:
         c.set_rho(np.zeros(33 * 32))
