@@ -17,12 +17,15 @@ the same charge), far larger than L2 (129 MB), so no L2 flush is needed.
           summed over ranks (replicas; one GPU each), max time over ranks.
   e2e     the same metric through the public C ABI with host buffers: every
           step uploads x, y, q (FP64, pinned) and downloads rho (FP64).
-  roofline  the deposit kernel alone: algorithmic bytes (8 B per particle
-          when every particle has the same charge, as here -- the charge stream
-          is not read -- else 12 B; + 12 B per cell: the int64 grid written, the
-          cell offsets read) / its mean CUDA-event duration, against the measured
-          HBM copy bandwidth in MEASURED_PEAKS.json.
-  summary   last on the line: per-kernel times and fractions of HBM, the
+  roofline  the deposit kernel alone: algorithmic bytes (16 B per particle:
+          x_rel, y_rel, q, cell key; + 8 B per cell: the int64 grid written once)
+          / its mean CUDA-event duration, against the measured HBM copy
+          bandwidth in MEASURED_PEAKS.json; frac_bytes_read is the same time
+          against the bytes the kernel reads (8 B per particle when every
+          particle has the same charge, as here -- neither the charge stream nor,
+          after a sort, the cell keys are read -- + 12 B per cell).
+  summary   last on the line: per-kernel times and fractions of HBM (at the
+          algorithmic bytes, and for the deposits at the bytes read), the
           per-scheme errors against the FP64 deposit, and the time-step,
           ensemble, warm-start and convolution headlines, rounded.
   cpu_baseline  the reference's FP64 CPU deposit on the host cores (rank 0);
@@ -67,6 +70,17 @@ BYTES_PER_PARTICLE_ESK = 20  # + vx, vy
 # do not read the charge stream: 4 B less per particle
 BYTES_Q = 4
 BYTES_PER_CELL = 12  # int64 rho written once + the u32 cell offsets read once
+# Algorithmic bytes per unit of work, the figures the roofline is quoted on
+# (independent of how a kernel lays out or skips its reads): a deposit reads
+# x_rel, y_rel, q (FP32) and the u32 cell key of each particle and writes the
+# int64 grid once, 16 B per particle + 8 B per cell; the Esirkepov schemes read
+# vx, vy too (24 B per particle; the current writes two grids). For the config
+# 1024x1024, 64 per cell: 1.0821e9 B per deposit, so 60 % of the measured HBM
+# copy bandwidth is a deposit of at most 0.270 ms. The bytes the sorted kernels
+# actually read (above) are reported beside it.
+ALG_BYTES_PER_PARTICLE = 16
+ALG_BYTES_PER_PARTICLE_ESK = 24
+ALG_BYTES_PER_CELL = 8
 # learned warm start for red-black Gauss-Seidel: 512x512, 64 particles per cell,
 # density 1 + 0.05*cos(2*pi*x/512), vth = 1 (the reference's charge convention,
 # total charge -1 and m = 1, with the neutralising background), dt = 0.1
@@ -384,10 +398,15 @@ def summary(res):
     out = {"kernels": {}}
     for k, v in ex.items():
         ms = v.get("kernel_ms", v.get("ms", v.get("ms_per_step")))
-        out["kernels"][k] = [r4(ms), r4(v.get("frac"))] if "frac" in v else r4(ms)
+        if "frac_bytes_read" in v:
+            out["kernels"][k] = [r4(ms), r4(v.get("frac")), r4(v["frac_bytes_read"])]
+        else:
+            out["kernels"][k] = [r4(ms), r4(v.get("frac"))] if "frac" in v else r4(ms)
     err = res.get("errors_vs_fp64") or {}
     out["errors_vs_fp64"] = {k: [r4(v["max_abs"]), r4(v["rel_l2"])] for k, v in err.items() if isinstance(v, dict)}
-    out["roofline_frac"] = r4((res.get("roofline") or {}).get("frac"))
+    rl = res.get("roofline") or {}
+    out["roofline_frac"] = r4(rl.get("frac"))
+    out["roofline_frac_bytes_read"] = r4(rl.get("frac_bytes_read"))
     ts = res.get("timestep_2048")
     if ts:
         out["timestep_2048"] = {"ms_per_step": r4(ts["ms_per_step"]), "steps": ts["steps"],
@@ -497,10 +516,13 @@ def run_gpu(args, d: Dist):
             ctx.deposit(s, ESK_DT, download=False)
         ms, cnt = ctx.profile_read("deposit")
         bpp = (BYTES_PER_PARTICLE_ESK if s == 3 else BYTES_PER_PARTICLE) - (BYTES_Q if q_uniform else 0)
+        abpp = ALG_BYTES_PER_PARTICLE_ESK if s == 3 else ALG_BYTES_PER_PARTICLE
         kms = ms / cnt
-        gbs = (bpp * n + BYTES_PER_CELL * G) / (kms / 1e3) / 1e9
+        gbs = (abpp * n + ALG_BYTES_PER_CELL * G) / (kms / 1e3) / 1e9
+        read_gbs = (bpp * n + BYTES_PER_CELL * G) / (kms / 1e3) / 1e9
         extras[f"{nm}_sorted"] = {"particles_per_s": n / (kms / 1e3), "kernel_ms": kms, "kernel_gbs": gbs,
-                                  "frac": gbs / peak, "bytes_per_particle": bpp}
+                                  "frac": gbs / peak, "frac_bytes_read": read_gbs / peak,
+                                  "bytes_per_particle_read": bpp}
         gpu_out[nm] = ctx.deposit(s, ESK_DT)
     sort_gbs = (48 * n + 4 * (G + 1)) / (sort_ms / 1e3) / 1e9
     extras["sort_random_to_cells"] = {"ms": sort_ms, "particles_per_s": n / (sort_ms / 1e3),
@@ -553,10 +575,12 @@ def run_gpu(args, d: Dist):
     for _ in range(20):
         ctx.deposit(SCHEMES["CIC"], ESK_DT, download=False)
     ms, cnt = ctx.profile_read("deposit")
-    gbs = (BYTES_PER_PARTICLE * n + BYTES_PER_CELL * G) / (ms / cnt / 1e3) / 1e9
+    gbs = (ALG_BYTES_PER_PARTICLE * n + ALG_BYTES_PER_CELL * G) / (ms / cnt / 1e3) / 1e9
+    read_gbs = (BYTES_PER_PARTICLE * n + BYTES_PER_CELL * G) / (ms / cnt / 1e3) / 1e9
     extras["CIC_sorted_per_particle_charges"] = {"particles_per_s": n / (ms / cnt / 1e3), "kernel_ms": ms / cnt,
                                                  "kernel_gbs": gbs, "frac": gbs / peak,
-                                                 "bytes_per_particle": BYTES_PER_PARTICLE}
+                                                 "frac_bytes_read": read_gbs / peak,
+                                                 "bytes_per_particle_read": BYTES_PER_PARTICLE}
     # restore the benchmark state: the random-order particles, cell-sorted
     ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
     ctx.sort()
@@ -588,7 +612,8 @@ def run_gpu(args, d: Dist):
     value = n * args.steps * d.ws / (ms_max / 1e3)
     kernel_ms = kms_tot / max(kcnt, 1)
     bpp_main = BYTES_PER_PARTICLE - (BYTES_Q if q_uniform else 0)
-    alg_bytes = bpp_main * n + BYTES_PER_CELL * G
+    read_bytes = bpp_main * n + BYTES_PER_CELL * G
+    alg_bytes = ALG_BYTES_PER_PARTICLE * n + ALG_BYTES_PER_CELL * G
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     traffic = traffic_from_profile()
 
@@ -654,7 +679,9 @@ def run_gpu(args, d: Dist):
                    "parallelism": f"replicas{d.ws}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "kernel": "deposit_cells<CIC>",
-                     "kernel_ms": kernel_ms, "algorithmic_bytes_per_launch": alg_bytes},
+                     "kernel_ms": kernel_ms, "algorithmic_bytes_per_launch": alg_bytes,
+                     "bytes_read_per_launch": read_bytes,
+                     "frac_bytes_read": read_bytes / (kernel_ms / 1e3) / 1e9 / peak},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "particles/s", "h2d_bytes_per_step": 24 * n,
                 "d2h_bytes_per_step": 8 * G, "steps": e2e_steps},
