@@ -261,10 +261,18 @@ typedef struct pic_run_config {
                               1 cubic extrapolation of the last three solutions; 2 extrapolation plus
                               the trained network's correction (pic_gpu_ws_*). Modes 1 and 2 need
                               pic_gpu_ws_init; until three solutions exist they start from phi. */
+    double sort_moved_fraction; /* 0: sorts follow sort_interval alone. > 0: also sort when the
+                              deposit of step s-2 found more than this fraction of the particles
+                              outside their cell of the last sort (read two steps behind, so the
+                              GPU never waits for the host); the interval, if > 0, still bounds
+                              the steps between sorts, and step 0 sorts unless the particles are
+                              already in cell order. Results do not depend on it. */
 } pic_run_config;
 /* Advances `steps` steps; history (steps entries, may be NULL) receives every
  * step's diagnostics (SimulationResult::*_history, simulation.hpp:49-60). */
 int pic_gpu_run(pic_ctx* ctx, const pic_run_config* cfg, int steps, pic_diag* history);
+/* Cell sorts performed on this context so far (pic_gpu_sort, and the sorts of pic_gpu_run). */
+int pic_gpu_sort_count(pic_ctx* ctx, long long* n);
 
 /* ---- deposit for callers that cannot allocate device memory ----
  *

@@ -1261,6 +1261,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
     uint32_t t = 0;
     int buf = 0;
     uint32_t cnt = 0;  // particles of the cell summed (KEYS: those still in it)
+    uint32_t moved = 0;  // KEYS: particles of this warp's cells that left them (warp-uniform)
     CellRun<S, QC> run;
     if constexpr (S == S_NGP && QC) run.A = __float2int_rn(a.qc * 16777216.0f);
     run.zero();
@@ -1333,6 +1334,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
             }
         }
         if constexpr (KEYS) {
+            moved += qn;
             if (qn) {  // the stage's particles that left their cell, one per lane
                 __syncwarp();
                 for (uint32_t i = (uint32_t)lane; i < qn; i += 32) {
@@ -1383,6 +1385,9 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
         buf = buf + 1 == NBUF ? 0 : buf + 1;
     }
     cp_async_wait<0>();
+    if constexpr (KEYS) {
+        if (lane == 0 && moved) atomicAdd(&a.st->moved, (unsigned long long)moved);
+    }
     __syncthreads();
     if (dense) return;
     for (int i = threadIdx.x; i < nloc; i += NW * 32) {

@@ -24,6 +24,7 @@ struct DevStats {
     unsigned int order_breaks;  // uploads: count of i with cell[i] < cell[i-1]
     unsigned int q_mixed;       // uploads: nonzero when the stored charges differ
     float q_first;              // uploads: the first particle's stored charge
+    unsigned long long moved;   // deposits between sorts: particles found outside their sorted cell
 };
 
 enum DevErr : int {
@@ -133,6 +134,7 @@ struct pic_ctx {
     int tile_user = 0;  // tile shape set by pic_gpu_set_tile (else chosen per deposit)
 
     long long launches = 0;
+    long long sorts = 0;  // cell sorts performed (pic_gpu_sort and the time step's)
 
     // optional CUDA-event records around named kernels (pic_gpu_profile_*)
     int prof_enabled = 0;

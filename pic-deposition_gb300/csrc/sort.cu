@@ -359,6 +359,7 @@ extern "C" int pic_gpu_sort(pic_ctx* c, uint32_t* keys_out, uint32_t* perm_out, 
     const int rc = sort_particles(c);
     prof_end(c);
     PIC_TRY(rc);
+    c->sorts++;
     if (keys_out && c->n)
         PIC_CUDA_TRY(cudaMemcpyAsync(keys_out, c->cell, c->n * 4, cudaMemcpyDeviceToHost, c->stream));
     if (perm_out && c->n)

@@ -52,6 +52,15 @@ __global__ void finalize_diag(const double* __restrict__ r, double vol, double* 
     *step = s + 1;
 }
 
+// moved[s] = the particles the step's deposit found outside their sorted cell
+// (step s = the diagnostics counter: the previous step's diagnostics are done)
+__global__ void take_moved(DevStats* st, unsigned long long* __restrict__ moved, const int* __restrict__ step,
+                           int steps) {
+    const int s = *step;
+    if (s < steps) moved[s] = st->moved;
+    st->moved = 0;
+}
+
 static int solve(pic_ctx* c, const pic_run_config* cfg) {
     if (cfg->poisson != 1) return poisson_fft(c);
     if (cfg->rbgs_warm > 0) PIC_TRY(ws_warm_guess(c, cfg->rbgs_warm));
@@ -73,9 +82,15 @@ static int record_step(pic_ctx* c, double* hist, int* step_ctr, int steps) {
 // kernel), then the previous step's diagnostics (the push leaves the velocities
 // unchanged); the last step's gather runs after the loop.
 static int one_step(pic_ctx* c, const pic_run_config* cfg, bool do_sort, double* hist, int* step_ctr, int steps,
-                    bool head) {
+                    bool head, unsigned long long* moved) {
+    auto count_moved = [&]() -> int {
+        if (!moved) return PIC_OK;
+        take_moved<<<1, 1, 0, c->stream>>>(c->dstats, moved, step_ctr, steps);
+        return check_launch(c, "take_moved");
+    };
     if (cfg->scheme == PIC_SCHEME_ESIRKEPOV) {
         PIC_TRY(deposit_rho(c, cfg->scheme, cfg->dt, cfg->background));
+        PIC_TRY(count_moved());
         PIC_TRY(solve(c, cfg));
         PIC_TRY(move(c, cfg->dt, false, true));
         PIC_TRY(move(c, cfg->dt, true, false));
@@ -89,6 +104,7 @@ static int one_step(pic_ctx* c, const pic_run_config* cfg, bool do_sort, double*
     }
     if (do_sort) PIC_TRY(sort_particles(c));
     PIC_TRY(deposit_rho(c, cfg->scheme, cfg->dt, cfg->background));
+    PIC_TRY(count_moved());
     return solve(c, cfg);
 }
 
@@ -151,13 +167,13 @@ struct StepGraph {
 };
 
 static int capture(pic_ctx* c, const pic_run_config* cfg, bool do_sort, double* hist, int* ctr, int steps,
-                   bool head, cudaGraphExec_t* out) {
+                   bool head, unsigned long long* moved, cudaGraphExec_t* out) {
     const int prof = c->prof_enabled;
     c->prof_enabled = 0;
     cudaGraph_t g = nullptr;
     const long long l0 = c->launches;
     PIC_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    const int rc = one_step(c, cfg, do_sort, hist, ctr, steps, head);
+    const int rc = one_step(c, cfg, do_sort, hist, ctr, steps, head, moved);
     const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->prof_enabled = prof;
     (do_sort ? c->graph_launches_sort : c->graph_launches_plain) = c->launches - l0;
@@ -181,34 +197,79 @@ int run_steps(pic_ctx* c, const pic_run_config* cfg, int steps, pic_diag* histor
     if (cfg->poisson == 1 && cfg->rbgs_warm > 0 && !c->ws)
         return fail(PIC_ERR_STATE, "rbgs_warm 1 and 2 need pic_gpu_ws_init");
     if (steps < 0) return fail(PIC_ERR_ARG, "steps < 0");
+    if (cfg->sort_interval < 0) return fail(PIC_ERR_ARG, "sort_interval < 0");
+    if (!(cfg->sort_moved_fraction >= 0.0 && cfg->sort_moved_fraction <= 1.0))
+        return fail(PIC_ERR_ARG, "sort_moved_fraction must be in [0, 1]");
     if (steps == 0) return PIC_OK;
     int rc = PIC_OK;
+    const bool by_moved = cfg->sort_moved_fraction > 0.0;
     double* hist = (double*)dalloc((size_t)steps * 6 * sizeof(double), &rc);
     if (!hist) return rc;
     int* ctr = (int*)dalloc(sizeof(int), &rc);
-    if (!ctr) {
-        dfree(hist);
-        return rc;
+    unsigned long long* moved = nullptr;     // per step, on the device
+    unsigned long long* moved_h = nullptr;   // the same, page-locked, copied after each step
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    if (ctr && by_moved) {
+        moved = (unsigned long long*)dalloc((size_t)steps * sizeof(unsigned long long), &rc);
+        if (moved && cudaHostAlloc((void**)&moved_h, (size_t)steps * sizeof(unsigned long long), 0) != cudaSuccess) {
+            moved_h = nullptr;
+            rc = fail(PIC_ERR_NOMEM, "pinned allocation");
+        }
+        for (int i = 0; i < 3 && rc == PIC_OK; ++i)
+            if (cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess)
+                rc = fail(PIC_ERR_CUDA, "cudaEventCreate");
     }
     std::vector<StepGraph> graphs;
     auto cleanup = [&]() {
         for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
         cudaStreamSynchronize(c->stream);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+        if (moved_h) cudaFreeHost(moved_h);
+        dfree(moved);
         dfree(hist);
         dfree(ctr);
     };
+    if (rc != PIC_OK) {
+        cleanup();
+        return rc;
+    }
     rc = [&]() -> int {
         PIC_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(int), c->stream));
+        PIC_CUDA_TRY(cudaMemsetAsync(&c->dstats->moved, 0, sizeof(unsigned long long), c->stream));
         PIC_TRY(ensure_fields(c));
         const int k = cfg->sort_interval;
         // the Gauss-Seidel stop is decided on the host, so those steps run eagerly
         const bool graph = cfg->use_graph && cfg->poisson == 0;
         const bool esk = cfg->scheme == PIC_SCHEME_ESIRKEPOV;
+        const double limit = cfg->sort_moved_fraction * (double)c->n;
+        int last_sort = -1;
         for (int s = 0; s < steps; ++s) {
-            const bool do_sort = k > 0 && (s % k) == 0;
+            bool do_sort = k > 0 && (s % k) == 0;
+            if (by_moved) {
+                // interval: steps since the last sort; step 0 sorts unless already in order
+                do_sort = (s == 0 && !c->sorted) || (k > 0 && last_sort >= 0 && s - last_sort >= k);
+                const int m = s - 2;  // the newest count the host may wait for without draining the GPU
+                if (!do_sort && m >= 0 && m > last_sort) {
+                    PIC_CUDA_TRY(cudaEventSynchronize(ev[m % 3]));
+                    do_sort = (double)moved_h[m] > limit;
+                }
+            }
+            if (do_sort) {
+                last_sort = s;
+                c->sorts++;
+            }
             const bool head = s > 0;  // the previous step's gather is pending (NGP/CIC/TSC)
+            auto after_step = [&]() -> int {
+                if (!by_moved) return PIC_OK;
+                PIC_CUDA_TRY(cudaMemcpyAsync(moved_h + s, moved + s, sizeof(unsigned long long),
+                                             cudaMemcpyDeviceToHost, c->stream));
+                PIC_CUDA_TRY(cudaEventRecord(ev[s % 3], c->stream));
+                return PIC_OK;
+            };
             if (!graph || s == 0) {
-                PIC_TRY(one_step(c, cfg, do_sort, hist, ctr, steps, head));
+                PIC_TRY(one_step(c, cfg, do_sort, hist, ctr, steps, head, moved));
+                PIC_TRY(after_step());
                 continue;
             }
             const Buffers now = buffers_of(c);
@@ -219,7 +280,7 @@ int run_steps(pic_ctx* c, const pic_run_config* cfg, int steps, pic_diag* histor
                 StepGraph sg;
                 sg.do_sort = do_sort;
                 sg.before = now;
-                PIC_TRY(capture(c, cfg, do_sort, hist, ctr, steps, head, &sg.exec));
+                PIC_TRY(capture(c, cfg, do_sort, hist, ctr, steps, head, moved, &sg.exec));
                 sg.after = buffers_of(c);  // the capture ran the host side: pointers as the graph leaves them
                 sg.kernels = do_sort ? c->graph_launches_sort : c->graph_launches_plain;
                 graphs.push_back(sg);
@@ -228,6 +289,7 @@ int run_steps(pic_ctx* c, const pic_run_config* cfg, int steps, pic_diag* histor
             PIC_CUDA_TRY(cudaGraphLaunch(g->exec, c->stream));
             set_buffers(c, g->after);
             c->launches += g->kernels;
+            PIC_TRY(after_step());
         }
         if (!esk) {  // the last step's gather and diagnostics
             PIC_TRY(move(c, cfg->dt, true, false));
@@ -252,4 +314,10 @@ extern "C" int pic_gpu_run(pic_ctx* c, const pic_run_config* cfg, int steps, pic
     if (!c || !cfg) return fail(PIC_ERR_ARG, "NULL argument");
     PIC_CUDA_TRY(cudaSetDevice(c->device));
     return run_steps(c, cfg, steps, history);
+}
+
+extern "C" int pic_gpu_sort_count(pic_ctx* c, long long* n) {
+    if (!c || !n) return fail(PIC_ERR_ARG, "NULL argument");
+    *n = c->sorts;
+    return PIC_OK;
 }

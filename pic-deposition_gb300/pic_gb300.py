@@ -93,10 +93,12 @@ class RunConfig(C.Structure):
     """pic_run_config (include/pic_gb300.h)."""
     _fields_ = [("scheme", C.c_int), ("poisson", C.c_int), ("dt", C.c_double), ("background", C.c_double),
                 ("sort_interval", C.c_int), ("use_graph", C.c_int), ("rbgs_tol", C.c_double),
-                ("rbgs_max_iters", C.c_int), ("rbgs_check_every", C.c_int), ("rbgs_warm", C.c_int)]
+                ("rbgs_max_iters", C.c_int), ("rbgs_check_every", C.c_int), ("rbgs_warm", C.c_int),
+                ("sort_moved_fraction", C.c_double)]
 
 
 _SIGS.append(("pic_gpu_run", [_vp, C.POINTER(RunConfig), C.c_int, C.POINTER(_Diag)]))
+_SIGS.append(("pic_gpu_sort_count", [_vp, C.POINTER(C.c_longlong)]))
 _SIGS.append(("pic_gpu_deposit_current", [_vp, C.c_double, _vp, _vp]))
 _SIGS.append(("pic_gpu_get_current_fixed", [_vp, _vp, _vp, _dp, _dp]))
 _SIGS.append(("pic_nn_conv3x3", [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]))
@@ -621,14 +623,23 @@ class Context:
                 "phi_diff": np.array([s.phi_diff for s in st])}
 
     def run(self, steps, scheme=1, dt=0.01, background=0.0, sort_interval=0, use_graph=False, poisson=0,
-            rbgs_tol=1e-8, rbgs_max_iters=100000, rbgs_check_every=64, rbgs_warm=0):
+            rbgs_tol=1e-8, rbgs_max_iters=100000, rbgs_check_every=64, rbgs_warm=0, sort_moved_fraction=0.0):
         """Advances `steps` time steps; returns the per-step diagnostics as a (steps, 6) array in
-        pic_diag order (charge_error, total_charge, integrated_rho, kinetic, field, total)."""
+        pic_diag order (charge_error, total_charge, integrated_rho, kinetic, field, total).
+        sort_moved_fraction > 0 also sorts when that fraction of the particles has left the
+        cells of the last sort (pic_run_config)."""
         cfg = RunConfig(int(scheme), int(poisson), float(dt), float(background), int(sort_interval),
-                        int(use_graph), float(rbgs_tol), int(rbgs_max_iters), int(rbgs_check_every), int(rbgs_warm))
+                        int(use_graph), float(rbgs_tol), int(rbgs_max_iters), int(rbgs_check_every), int(rbgs_warm),
+                        float(sort_moved_fraction))
         hist = (_Diag * max(steps, 1))()
         _check(lib().pic_gpu_run(self.h, C.byref(cfg), int(steps), hist))
         return np.array([[getattr(h, k) for k, _ in _Diag._fields_] for h in hist[:steps]])
+
+    def sort_count(self) -> int:
+        """Cell sorts performed on this context (pic_gpu_sort_count)."""
+        n = C.c_longlong()
+        _check(lib().pic_gpu_sort_count(self.h, C.byref(n)))
+        return n.value
 
     def diagnostics(self) -> dict:
         d = _Diag()

@@ -108,6 +108,36 @@ def test_kinetic_sum_and_charge_cache(pg, port):
     assert h2[0, 1] == pytest.approx(np.sum(q2), rel=1e-6) and h2[0, 1] != h[0, 1]
 
 
+def test_sort_by_moved_fraction(pg, port):
+    """Sorts triggered by the measured disorder (pic_run_config.sort_moved_fraction)
+    give the fixed interval's particles and grid quantities bit for bit; a lower
+    threshold sorts more often; an out-of-range threshold is rejected."""
+    nx = ny = 64
+    p = port.init_particles(0, nx, ny, 1.0, 1.0, 50000, p0=1.0, seed=3)
+    outs, sorts = [], {}
+    for k, f, graph in ((3, 0.0, True), (0, 0.05, True), (0, 0.95, False), (8, 0.6, True)):
+        with start(pg, nx, ny, 1.0, 1.0, p) as c:
+            n0 = c.sort_count()
+            h = c.run(30, scheme=TSC, dt=0.004, sort_interval=k, use_graph=graph, sort_moved_fraction=f)
+            sorts[(k, f)] = c.sort_count() - n0
+            lay = c.device_layout()
+            if f == 0.95:
+                with pytest.raises(pg.PicError) as e:
+                    c.run(2, scheme=TSC, dt=0.004, sort_moved_fraction=1.5)
+                assert e.value.code == -1
+        key = np.lexsort((lay["vy"], lay["vx"], lay["yr"], lay["xr"], lay["cell"]))
+        outs.append((h, {kk: v[key] for kk, v in lay.items()}))
+    for h, lay in outs[1:]:
+        for kk in lay:
+            assert np.array_equal(lay[kk], outs[0][1][kk])
+        for col in (0, 1, 2, 4):
+            assert np.array_equal(h[:, col], outs[0][0][:, col])
+        assert np.allclose(h[:, 3], outs[0][0][:, 3], rtol=1e-13, atol=0)
+    assert sorts[(3, 0.0)] == 10
+    assert sorts[(0, 0.05)] > sorts[(0, 0.95)] >= 1
+    assert sorts[(8, 0.6)] >= 30 // 8
+
+
 def test_rbgs_matches_oracle(pg, port):
     nx, ny = 64, 48
     rng = np.random.default_rng(0)
