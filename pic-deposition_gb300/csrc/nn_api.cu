@@ -50,7 +50,7 @@ extern "C" int pic_nn_conv3x3(int op, int batch, int H, int W, int cin, int cout
     PIC_CUDA_TRY(cudaMemset(derr, 0, sizeof(int)));
     if (op == 3) {
         uint16_t* ddy = d.alloc<uint16_t>(P * cout * 2, &rc);
-        const long long units = (long long)P / 64;
+        const long long units = picnn::wgrad_units(batch, H, W);
         const int grid = picnn::wgrad_grid(units);
         const int upc = (int)((units + grid - 1) / grid);
         const int g2 = (int)((units + upc - 1) / upc);

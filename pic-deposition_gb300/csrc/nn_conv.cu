@@ -289,47 +289,155 @@ __global__ void __launch_bounds__(THREADS) conv3x3_kernel(ConvLaunch a) {
 // ---------------------------------------------------------------------------
 // weight gradient
 // ---------------------------------------------------------------------------
-template <int CIN, int COUT>
-struct WgSmem {
-    static constexpr int MPAD = ((9 * CIN + 1 + 127) / 128) * 128;
-    static constexpr int MT = MPAD / 128;
-    static constexpr int LBO_A = MPAD * 16;
-    static constexpr int ABYTES = 8 * LBO_A;
-    static constexpr int BBYTES = 8 * COUT * 16;
-    static constexpr int OFF_B = 2 * ABYTES;
-    static constexpr int OFF_RAWX = OFF_B + 2 * BBYTES;
-    static constexpr int RAWX = 3 * 66 * CIN * 2;
-    static constexpr int OFF_RAWD = OFF_RAWX + RAWX;
-    static constexpr int BYTES = OFF_RAWD + 64 * COUT * 2;
-};
+// Both operands are MN-major: A[m][k] = x with m = (row offset, channel) and
+// k = pixel, B[k][n] = dy with n = output channel. Staged as 8-channel planes
+// (16 bytes per pixel slot) they are the canonical MN-major no-swizzle layout:
+// a core matrix is 8 pixels (K, 16 B apart) of 8 channels (MN, contiguous); K
+// core matrices are 128 B apart (LBO), MN core matrices one plane apart (SBO).
+// With the staged x rows of a block one after the other, the 16 MN core
+// matrices of an M = 128 operand starting at row i are rows i .. i + 128/CIN - 1:
+// rows i, i+1, i+2 are the taps dy = -1, 0, 1 of output row i (the rest is
+// discarded), and the tap dx moves the start by one 16-byte pixel slot. The
+// bias gradient is one more MMA per K step, of a constant all-ones A.
+//
+// Staging: a row of a block is one TMA copy (cp.async.bulk.tensor) of a box of
+// 8 channels x 34 (or 40) pixels x planes through a 5-D view of the NHWC tensor whose
+// pixel stride is the pixel's size and whose plane stride is 16 bytes, so the
+// box lands plane by plane; the periodic row wrap is the row coordinate. The two
+// segments at the ends of an image row, whose pixel halo wraps around, are
+// staged with cp.async by three warps instead.
+constexpr int WG_ROWS = 8;    // output rows per block
+constexpr int WG_PX = 32;     // output pixels per block (one K segment)
+constexpr int WG_SLOTS = 34;  // x pixels used: x0-1 .. x0+32
+constexpr int WG_DPLANE = WG_PX * 16;
+constexpr int WG_NBUF = 2;    // blocks in the shared-memory ring
+constexpr int WG_ONES = 16 * 256;  // all-ones A operand: 16 MN x 2 K core matrices
 
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(THREADS) wgrad_kernel(WgradLaunch a) {
+struct WgSmem {
+    static constexpr int G = 128 / CIN;                 // x rows spanned by one M = 128 operand
+    static constexpr int XROWS = WG_ROWS + G - 1;       // staged x rows per block
+    // x pixels per TMA box: the 34 used, or 40 where 34 would leave the rows off
+    // the 128-byte alignment of a TMA destination
+    static constexpr int XBOX = ((CIN / 8) * 34 * 16) % 128 == 0 ? 34 : 40;
+    static constexpr int XPLANE = XBOX * 16;
+    static constexpr int XROW = (CIN / 8) * XPLANE;     // bytes per staged x row
+    static constexpr int DROW = (COUT / 8) * WG_DPLANE;
+    static constexpr int XBYTES = XROWS * XROW;
+    static constexpr int DBYTES = WG_ROWS * DROW;
+    static constexpr int BUF = (XBYTES + DBYTES + 127) / 128 * 128;
+    static constexpr int OFF_ONES = WG_NBUF * BUF;
+    static constexpr int BYTES = OFF_ONES + WG_ONES;
+};
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all_groups() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint32_t a, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map, int c1, int c2, int c3, int c4,
+                                            uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(mbar)
+        : "memory");
+}
+
+// Instruction descriptor of kind::f16 with both operands MN-major.
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int m, int n) {
+    return idesc_bf16(m, n) | (1u << 15) | (1u << 16);
+}
+
+struct WgBlock {
+    int b, y0, x0, rows;
+    bool edge;  // the x halo wraps around the image row: staged with cp.async
+};
+
+__device__ __forceinline__ WgBlock wg_block(const WgradLaunch& a, long long blk) {
+    const int segs = a.W / WG_PX, yblocks = (a.H + WG_ROWS - 1) / WG_ROWS;
+    WgBlock k;
+    const int seg = (int)(blk % segs);
+    const long long r2 = blk / segs;
+    k.y0 = (int)(r2 % yblocks) * WG_ROWS;
+    k.b = (int)(r2 / yblocks);
+    k.x0 = seg * WG_PX;
+    k.rows = min(WG_ROWS, a.H - k.y0);
+    k.edge = seg == 0 || seg == segs - 1;
+    return k;
+}
+
+// cp.async staging of a block by the 96 producer threads (pt = 0..95): the same
+// layout as the TMA boxes (slots past 33 of a plane, if any, are not written or read).
+template <int CIN, int COUT>
+__device__ __forceinline__ void wg_stage_cp(const WgradLaunch& a, const WgBlock& k, uint32_t buf, int pt) {
     using L = WgSmem<CIN, COUT>;
-    constexpr uint32_t IDESC = idesc_bf16(128, COUT);
-    constexpr uint32_t TCOLS = tmem_cols(L::MT * COUT);
+    constexpr int XP = CIN / 8, DP = COUT / 8;
+    const size_t img = (size_t)k.b * a.H;
+    int ystart = (k.y0 - 1) % a.H;
+    if (ystart < 0) ystart += a.H;
+    for (int u = pt; u < XP * WG_SLOTS; u += 96) {
+        const int sl = u / XP, j = u % XP;
+        int xx = k.x0 - 1 + sl;
+        if (xx < 0) xx += a.W;
+        if (xx >= a.W) xx -= a.W;
+        const uint16_t* col = a.x + (size_t)xx * CIN + j * 8;
+        int yy = ystart;
+#pragma unroll
+        for (int r = 0; r < L::XROWS; ++r) {
+            cp_async16(buf + (uint32_t)(r * L::XROW + j * L::XPLANE + sl * 16), col + (img + yy) * (size_t)a.W * CIN);
+            if (++yy == a.H) yy = 0;
+        }
+    }
+    for (int u = pt; u < DP * WG_PX; u += 96) {
+        const int sl = u / DP, j = u % DP;
+        const uint16_t* col = a.dy + ((img + k.y0) * a.W + k.x0 + sl) * COUT + j * 8;
+        for (int r = 0; r < k.rows; ++r)
+            cp_async16(buf + (uint32_t)(L::XBYTES + r * L::DROW + j * WG_DPLANE + sl * 16), col + (size_t)r * a.W * COUT);
+    }
+}
+
+// Warp-specialised pipeline over a ring of WG_NBUF buffers. Warps 1-3 are the
+// producers (lane 0 of warp 1 issues the TMA copies; all three warps stage the
+// edge blocks with cp.async); lane 0 of warp 0 issues the MMAs. full[b] takes one
+// arrival from every producer thread for every block (after its cp.async copies
+// landed; the TMA issuer's arrival carries the expected bytes) and says buffer b
+// holds a block; empty[b] (the MMAs' commit) says the tensor cores are done with
+// it. Every producer thread waits on empty and arrives on full for every block,
+// so no thread is ever more than one phase away from a barrier it waits on (a
+// parity wait needs that), and no producer waits for another, so a wait that
+// runs out cannot strand the rest.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(THREADS) wgrad_kernel(const __grid_constant__ WgradLaunch a) {
+    using L = WgSmem<CIN, COUT>;
+    constexpr uint32_t IDESC = idesc_bf16_mn(128, COUT);
+    constexpr uint32_t TCOLS = tmem_cols(4 * COUT);
+    constexpr int XP = CIN / 8, DP = COUT / 8;
+    constexpr int MPAD = 9 * CIN + 1;
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t full[WG_NBUF], empty[WG_NBUF];
     __shared__ uint32_t tmem_slot;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int halves = a.W / 64;
-    const long long total = (long long)a.batch * a.H * halves;
-    const long long u_begin = (long long)blockIdx.x * a.units_per_cta;
-    const long long u_end = min(total, u_begin + a.units_per_cta);
-    const uint32_t s_a = smem_addr(smem);
-    const uint32_t s_b = s_a + L::OFF_B;
-    const uint16_t* rawx = reinterpret_cast<const uint16_t*>(smem + L::OFF_RAWX);
-    const uint16_t* rawd = reinterpret_cast<const uint16_t*>(smem + L::OFF_RAWD);
-    float* part = a.partials + (size_t)blockIdx.x * L::MPAD * COUT;
+    const long long total = (long long)a.batch * ((a.H + WG_ROWS - 1) / WG_ROWS) * (a.W / WG_PX);
+    const long long k_begin = (long long)blockIdx.x * a.units_per_cta;
+    const int nk = (int)max(0ll, min(total, k_begin + a.units_per_cta) - k_begin);
+    const uint32_t s0 = smem_addr(smem);
+    float* part = a.partials + (size_t)blockIdx.x * MPAD * COUT;
 
-    {  // zero both A buffers once: rows past the bias row stay zero
-        uint4* z = reinterpret_cast<uint4*>(smem);
-        for (int i = tid; i < 2 * L::ABYTES / 16; i += THREADS) z[i] = make_uint4(0, 0, 0, 0);
+    {  // the all-ones operand of the bias MMAs (BF16 1.0)
+        uint4* o = reinterpret_cast<uint4*>(smem + L::OFF_ONES);
+        for (int i = tid; i < WG_ONES / 16; i += THREADS) o[i] = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);
     }
+    fence_async_smem();
     if (tid == 0) {
-        mbar_init(smem_addr(&mbar[0]), 1);
-        mbar_init(smem_addr(&mbar[1]), 1);
+        for (int i = 0; i < WG_NBUF; ++i) {
+            mbar_init(smem_addr(&full[i]), 96);
+            mbar_init(smem_addr(&empty[i]), 1);
+        }
     }
     if (warp == 0) tmem_alloc(smem_addr(&tmem_slot), TCOLS);
     tc_fence_before();
@@ -337,98 +445,104 @@ __global__ void __launch_bounds__(THREADS) wgrad_kernel(WgradLaunch a) {
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
 
-    bool ok = true;
-    int k = 0;
-    for (long long u = u_begin; u < u_end; ++u, ++k) {
-        const int half = (int)(u % halves);
-        const long long rest = u / halves;
-        const int y = (int)(rest % a.H);
-        const int b = (int)(rest / a.H);
-        const int x0 = half * 64;
-        // raw rows: x at y-1..y+1, pixels x0-1..x0+64; dy at y, pixels x0..x0+63
-        for (int t = tid; t < 3 * 66 * (CIN / 8); t += THREADS) {
-            const int j = t % (CIN / 8), rs = t / (CIN / 8), s = rs % 66, r = rs / 66;
-            const int yy = ((y + r - 1) % a.H + a.H) % a.H;
-            int xx = x0 - 1 + s;
-            if (xx < 0) xx += a.W;
-            if (xx >= a.W) xx -= a.W;
-            cp_async16(s_a + L::OFF_RAWX + (uint32_t)(((r * 66 + s) * CIN + j * 8) * 2),
-                       a.x + (((size_t)b * a.H + yy) * a.W + xx) * CIN + j * 8);
-        }
-        for (int t = tid; t < 64 * (COUT / 8); t += THREADS) {
-            const int j = t % (COUT / 8), s = t / (COUT / 8);
-            cp_async16(s_a + L::OFF_RAWD + (uint32_t)((s * COUT + j * 8) * 2),
-                       a.dy + (((size_t)b * a.H + y) * a.W + x0 + s) * COUT + j * 8);
-        }
-        cp_async_wait_all();
-        const int buf = k & 1;
-        bool w = true;
-        if (k >= 2) w = mbar_wait(smem_addr(&mbar[buf]), ((k - 2) >> 1) & 1);
-        ok = __syncthreads_and(w);
-        if (!ok) break;
-        tc_fence_after();
-        uint8_t* abuf = smem + buf * L::ABYTES;
-        for (int t = tid; t < 9 * CIN * 8 + 8; t += THREADS) {
-            uint32_t p[4];
-            int m, kc;
-            if (t < 9 * CIN * 8) {
-                const int ci = t % CIN, rest2 = t / CIN;
-                kc = rest2 % 8;
-                const int tap = rest2 / 8;
-                m = tap * CIN + ci;
-                const int r = tap / 3, dx = tap % 3;
-                const uint16_t* src = rawx + (r * 66 + kc * 8 + dx) * CIN + ci;
-#pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    p[e] = (uint32_t)src[(2 * e) * CIN] | ((uint32_t)src[(2 * e + 1) * CIN] << 16);
-            } else {
-                kc = t - 9 * CIN * 8;
-                m = 9 * CIN;
-#pragma unroll
-                for (int e = 0; e < 4; ++e) p[e] = 0x3F803F80u;  // BF16 1.0, 1.0
+    int ok = 1;
+    if (warp > 0) {
+        const int pt = tid - 32;
+        for (int k = 0; k < nk; ++k) {
+            const int bsel = k % WG_NBUF;
+            const uint32_t buf = s0 + (uint32_t)(bsel * L::BUF);
+            const uint32_t fb = smem_addr(&full[bsel]);
+            const WgBlock blk = wg_block(a, k_begin + k);
+            if (k >= WG_NBUF && !mbar_wait(smem_addr(&empty[bsel]), ((k / WG_NBUF) - 1) & 1)) {
+                ok = 0;
+                break;
             }
-            *reinterpret_cast<uint4*>(abuf + kc * L::LBO_A + m * 16) = make_uint4(p[0], p[1], p[2], p[3]);
-        }
-        uint8_t* bbuf = smem + L::OFF_B + buf * L::BBYTES;
-        for (int t = tid; t < 8 * COUT; t += THREADS) {
-            const int co = t % COUT, kc = t / COUT;
-            const uint16_t* src = rawd + (kc * 8) * COUT + co;
-            uint32_t p[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) p[e] = (uint32_t)src[(2 * e) * COUT] | ((uint32_t)src[(2 * e + 1) * COUT] << 16);
-            *reinterpret_cast<uint4*>(bbuf + kc * COUT * 16 + co * 16) = make_uint4(p[0], p[1], p[2], p[3]);
-        }
-        fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            tc_fence_after();
-            const uint32_t a0 = s_a + buf * L::ABYTES, b0 = s_b + buf * L::BBYTES;
-#pragma unroll
-            for (int mt = 0; mt < L::MT; ++mt)
-#pragma unroll
-                for (int s = 0; s < 4; ++s) {
-                    const uint64_t ad = umma_desc(a0 + mt * 128 * 16 + s * 2 * L::LBO_A, L::LBO_A, 128);
-                    const uint64_t bd = umma_desc(b0 + s * 2 * COUT * 16, COUT * 16, 128);
-                    mma_bf16(tmem + mt * COUT, ad, bd, IDESC, (k > 0 || s > 0) ? 1u : 0u);
+            if (blk.edge) {
+                wg_stage_cp<CIN, COUT>(a, blk, buf, pt);
+                cp_async_commit();
+                cp_async_wait_all_groups();
+                fence_async_smem();
+                mbar_arrive(fb);
+            } else if (pt != 0) {
+                mbar_arrive(fb);
+            } else {
+                mbar_arrive_tx(fb, (uint32_t)(L::XROWS * L::XROW + blk.rows * L::DROW));
+                int yy = (blk.y0 - 1) % a.H;
+                if (yy < 0) yy += a.H;
+                for (int r = 0; r < L::XROWS; ++r) {
+                    tma_load_5d(buf + (uint32_t)(r * L::XROW), &a.tmx, blk.x0 - 1, 0, yy, blk.b, fb);
+                    if (++yy == a.H) yy = 0;
                 }
-            mma_commit(smem_addr(&mbar[buf]));
+                for (int r = 0; r < blk.rows; ++r)
+                    tma_load_5d(buf + (uint32_t)(L::XBYTES + r * L::DROW), &a.tmdy, blk.x0, 0, blk.y0 + r, blk.b, fb);
+            }
+        }
+    } else if (lane == 0) {
+        bool first = true;
+        const uint64_t ones = umma_desc(s0 + (uint32_t)L::OFF_ONES, 128, 256);
+        for (int k = 0; k < nk; ++k) {
+            const int bsel = k % WG_NBUF;
+            const uint32_t buf = s0 + (uint32_t)(bsel * L::BUF);
+            if (!mbar_wait(smem_addr(&full[bsel]), (k / WG_NBUF) & 1)) {
+                ok = 0;
+                break;
+            }
+            tc_fence_after();
+            const int rows = wg_block(a, k_begin + k).rows;
+            // descriptors advance by (bytes >> 4) in their start-address field
+            const uint64_t a0 = umma_desc(buf, 128, L::XPLANE);
+            const uint64_t b0 = umma_desc(buf + (uint32_t)L::XBYTES, 128, WG_DPLANE);
+            for (int i = 0; i < rows; ++i) {
+#pragma unroll
+                for (int kk = 0; kk < WG_PX / 16; ++kk) {
+                    const uint64_t bd = b0 + (uint64_t)((i * L::DROW + 16 * kk * 16) >> 4);
+                    const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+#pragma unroll
+                    for (int dx = 0; dx < 3; ++dx) {
+                        const uint64_t ad = a0 + (uint64_t)((i * L::XROW + (16 * kk + dx) * 16) >> 4);
+                        mma_bf16(tmem + (uint32_t)(dx * COUT), ad, bd, IDESC, acc);
+                    }
+                    mma_bf16(tmem + (uint32_t)(3 * COUT), ones, bd, IDESC, acc);
+                }
+                first = false;
+            }
+            mma_commit(smem_addr(&empty[bsel]));
         }
     }
-    if (ok && k > 0) {
-        const int last = k - 1;
-        ok = __syncthreads_and(mbar_wait(smem_addr(&mbar[last & 1]), (last >> 1) & 1));
+    cp_async_wait_all_groups();
+    __syncwarp();
+    ok = __syncthreads_and(ok);
+    if (ok && nk > 0) {
+        const int last = nk - 1;
+        ok = __syncthreads_and(mbar_wait(smem_addr(&empty[last % WG_NBUF]), (last / WG_NBUF) & 1));
         if (ok) {
             tc_fence_after();
-            for (int mt = 0; mt < L::MT; ++mt) {
-                float v[COUT];
-                tmem_load<COUT>(tmem + ((uint32_t)(warp * 32) << 16) + mt * COUT, v);
-                float* row = part + (size_t)(mt * 128 + warp * 32 + lane) * COUT;
+            // TMEM lane m = (row offset dyi, channel ci); column dx * COUT + co;
+            // columns 3 * COUT + co: the bias gradient (every lane the same)
+            if (warp * 32 < 3 * CIN) {
+                const int m = warp * 32 + lane, dyi = m / CIN, ci = m % CIN;
 #pragma unroll
-                for (int c = 0; c < COUT; ++c) row[c] = v[c];
+                for (int dx = 0; dx < 3; ++dx) {
+                    float v[COUT];
+                    tmem_load<COUT>(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(dx * COUT), v);
+                    if (dyi < 3) {
+                        float* row = part + (size_t)((dyi * 3 + dx) * CIN + ci) * COUT;
+#pragma unroll
+                        for (int c = 0; c < COUT; ++c) row[c] = v[c];
+                    }
+                }
+            }
+            if (warp == 0) {
+                float v[COUT];
+                tmem_load<COUT>(tmem + (uint32_t)(3 * COUT), v);
+                if (lane == 0) {
+#pragma unroll
+                    for (int c = 0; c < COUT; ++c) part[(size_t)9 * CIN * COUT + c] = v[c];
+                }
             }
         }
     } else if (ok) {
-        for (int i = tid; i < L::MPAD * COUT; i += THREADS) part[i] = 0.0f;
+        for (int i = tid; i < MPAD * COUT; i += THREADS) part[i] = 0.0f;
     }
     if (!ok && tid == 0) atomicExch(a.err, 1);
     tc_fence_before();
@@ -492,11 +606,51 @@ int launch_conv_t(const ConvLaunch& a, cudaStream_t s) {
     return e == cudaSuccess ? PIC_OK : picgb::cuda_fail(e, "conv3x3_kernel launch");
 }
 
+typedef CUresult (*TensorMapEncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                           const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                           CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int tensor_map_encoder(TensorMapEncodeTiledFn* out) {
+    static TensorMapEncodeTiledFn fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        const cudaError_t e =
+            cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", (void**)&fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) {
+            fn = nullptr;
+            return picgb::fail(PIC_ERR_UNSUPPORTED, "the driver does not provide cuTensorMapEncodeTiled");
+        }
+    }
+    *out = fn;
+    return PIC_OK;
+}
+
+// 5-D view of an NHWC BF16 tensor with C channels: (8 channels, pixel, 8-channel
+// plane, row, image), pixel stride C * 2 bytes and plane stride 16 bytes, and a
+// box of 8 channels x `px` pixels x all planes of one row, which lands in shared
+// memory as planes of `px` 16-byte pixel slots.
+int encode_planes_map(CUtensorMap* m, const uint16_t* base, int C, int batch, int H, int W, int px) {
+    TensorMapEncodeTiledFn enc;
+    PIC_TRY(tensor_map_encoder(&enc));
+    const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)(C / 8), (cuuint64_t)H, (cuuint64_t)batch};
+    const cuuint64_t strides[4] = {(cuuint64_t)C * 2, 16, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    const cuuint32_t box[5] = {8, (cuuint32_t)px, (cuuint32_t)(C / 8), 1, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<uint16_t*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return picgb::fail(PIC_ERR_CUDA, "cuTensorMapEncodeTiled failed for the weight gradient");
+    return PIC_OK;
+}
+
 template <int CIN, int COUT>
-int launch_wgrad_t(const WgradLaunch& a, int grid, cudaStream_t s) {
+int launch_wgrad_t(const WgradLaunch& a0, int grid, cudaStream_t s) {
     using L = WgSmem<CIN, COUT>;
     const int attr = picgb::opt_in_dynamic_smem((const void*)wgrad_kernel<CIN, COUT>, L::BYTES);
     if (attr != PIC_OK) return attr;
+    WgradLaunch a = a0;
+    PIC_TRY(encode_planes_map(&a.tmx, a.x, CIN, a.batch, a.H, a.W, L::XBOX));
+    PIC_TRY(encode_planes_map(&a.tmdy, a.dy, COUT, a.batch, a.H, a.W, WG_PX));
     wgrad_kernel<CIN, COUT><<<grid, THREADS, L::BYTES, s>>>(a);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PIC_OK : picgb::cuda_fail(e, "wgrad_kernel launch");
@@ -540,8 +694,8 @@ int wgrad_grid(long long units) {
 }
 
 int launch_wgrad(const WgradLaunch& a, int cin, int cout, int grid, cudaStream_t s) {
-    if (a.W % 64 != 0 || a.W <= 0 || a.H <= 0 || a.batch <= 0 || grid <= 0)
-        return picgb::fail(PIC_ERR_ARG, "weight gradient needs W a multiple of 64");
+    if (a.W % WG_PX != 0 || a.W <= 0 || a.H <= 0 || a.batch <= 0 || grid <= 0)
+        return picgb::fail(PIC_ERR_ARG, "weight gradient needs W a multiple of 32");
     if (cin == 16 && cout == 16) return launch_wgrad_t<16, 16>(a, grid, s);
     if (cin == 16 && cout == 32) return launch_wgrad_t<16, 32>(a, grid, s);
     if (cin == 32 && cout == 16) return launch_wgrad_t<32, 16>(a, grid, s);

@@ -1,12 +1,13 @@
 // 3x3 periodic convolutions on the tensor cores (tcgen05, BF16 in, FP32 accumulate).
 //
 // Tensors are NHWC BF16 with C in {16, 32}; W a multiple of 128 (forward and
-// input-gradient kernels) and of 64 (weight-gradient kernel). Weights in
+// input-gradient kernels) and of 32 (weight-gradient kernel). Weights in
 // "math" layout are FP32 w[tap][cout][cin], tap = (dy+1)*3 + (dx+1), and the
 // forward convolution is
 //     y[b,y,x,co] = bias[co] + sum_{dy,dx,ci} x[b,(y+dy)%H,(x+dx)%W,ci] * w[tap][co][ci].
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -36,15 +37,17 @@ struct WgradLaunch {
     const uint16_t* dy;  // gradient at the layer output, NHWC cout channels
     float* partials;     // [grid][mpad][cout]
     int batch, H, W;
-    int units_per_cta;   // 64-pixel half rows per CTA
+    int units_per_cta;   // blocks (8 rows x 32 pixels of one image) per CTA
     int* err;
+    CUtensorMap tmx, tmdy;  // TMA views of x and dy (filled by launch_wgrad)
 };
 
 // Bytes of a weight image for (cin, cout).
 inline size_t wimg_bytes(int cin, int cout) { return (size_t)9 * cin * cout * 2; }
-// Rows of the weight-gradient GEMM: 9*cin taps-by-channels, one row of ones
-// (the bias gradient), padded to whole 128-row tiles.
-inline int wgrad_mpad(int cin) { return ((9 * cin + 1 + 127) / 128) * 128; }
+// Rows of a weight-gradient partial sum: 9*cin taps-by-channels, then the bias.
+inline int wgrad_mpad(int cin) { return 9 * cin + 1; }
+// Blocks of the weight-gradient kernel: 8 rows x 32 pixels of one image.
+inline long long wgrad_units(int batch, int H, int W) { return (long long)batch * ((H + 7) / 8) * (W / 32); }
 
 // Forward convolution (transpose = 0) or the input gradient of layer (cin, cout)
 // (transpose = 1: w'[tap][ci][co] = w[8 - tap][co][ci]) as a weight image.
@@ -55,7 +58,7 @@ int launch_conv(const ConvLaunch& a, int kcin, int kcout, int epilogue, cudaStre
 int launch_wgrad(const WgradLaunch& a, int cin, int cout, int grid, cudaStream_t s);
 // dw[tap][co][ci] and db[co] from the partial sums of `grid` CTAs (fixed order).
 int reduce_wgrad(const float* partials, int grid, int cin, int cout, float* dw, float* db, cudaStream_t s);
-// CTAs the weight-gradient kernel uses for a problem of `units` half rows.
+// CTAs the weight-gradient kernel uses for a problem of `units` blocks.
 int wgrad_grid(long long units);
 
 }  // namespace picnn

@@ -249,7 +249,7 @@ int ws_forward(pic_ctx* c, int nb) {
 int ws_backward(pic_ctx* c, int nb) {
     WsState* s = c->ws;
     const int rows = nb >= 4 ? 16 : 8;
-    const long long units = (long long)nb * s->P / 64;
+    const long long units = picnn::wgrad_units(nb, s->H, s->W);
     const int grid0 = picnn::wgrad_grid(units);
     const int upc = (int)((units + grid0 - 1) / grid0);
     const int grid = (int)((units + upc - 1) / upc);
@@ -305,7 +305,10 @@ int ensure_batch(pic_ctx* c, int nb) {
     if (!rc) s->dz16 = (uint16_t*)dalloc((size_t)nb * P * 16 * 2, &rc);
     if (!rc) s->dza = (uint16_t*)dalloc((size_t)nb * P * 32 * 2, &rc);
     if (!rc) s->dzb = (uint16_t*)dalloc((size_t)nb * P * 32 * 2, &rc);
-    if (!rc) s->partials = (float*)dalloc((size_t)picnn::wgrad_grid((long long)nb * P / 64) * 384 * 32 * 4, &rc);
+    if (!rc)
+        s->partials = (float*)dalloc((size_t)picnn::wgrad_grid(picnn::wgrad_units(nb, s->H, s->W)) *
+                                         picnn::wgrad_mpad(32) * 32 * 4,
+                                     &rc);
     if (rc) return rc;
     s->batch_cap = nb;
     return PIC_OK;

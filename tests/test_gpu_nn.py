@@ -93,3 +93,19 @@ def test_weight_gradient(port, pg, cin, cout, shape):
     mag_w, mag_b = port.conv_wgrad(port.bf16(np.abs(port.from_bf16(x))), port.bf16(np.abs(port.from_bf16(g))))
     assert np.all(np.abs(dw - want_w) <= mag_w * 2.0 ** -16 + 1e-30)
     assert np.all(np.abs(db - want_b) <= mag_b * 2.0 ** -16 + 1e-30)
+
+
+@pytest.mark.parametrize("cin,cout", [(32, 32), (32, 16), (16, 32)])
+def test_weight_gradient_many_blocks_per_cta(port, pg, cin, cout):
+    """4 x 96 x 512 pixels: 768 blocks of 8 rows x 32 pixels on at most 304
+    CTAs, so CTAs run several blocks through their ring of two staging buffers
+    (TMA copies for the interior of a row, cp.async for its two ends)."""
+    rng = np.random.default_rng(7 + cin + cout)
+    shape = (4, 96, 512)
+    x = port.bf16(rng.normal(size=shape + (cin,)))
+    g = port.bf16(rng.normal(size=shape + (cout,)))
+    dw, db = pg.nn_conv3x3(pg.NN_WGRAD, x, aux=g, cin=cin, cout=cout)
+    want_w, want_b = port.conv_wgrad(x, g)
+    mag_w, mag_b = port.conv_wgrad(port.bf16(np.abs(port.from_bf16(x))), port.bf16(np.abs(port.from_bf16(g))))
+    assert np.all(np.abs(dw - want_w) <= mag_w * 2.0 ** -16 + 1e-30)
+    assert np.all(np.abs(db - want_b) <= mag_b * 2.0 ** -16 + 1e-30)
