@@ -1135,6 +1135,57 @@ __device__ __noinline__ void stale_to_global(const DepArgs& a, uint32_t key, flo
     particle_to_global<S, QC>(a, key, rx, ry, qn, vxx, vyy, p);
 }
 
+// A particle that left its cell since the sort, added to the CTA's tile
+// accumulators when its frame lies within them: its cell at most one cell
+// outside the tile (the accumulators have a halo one cell wider than the
+// tile's own frames need, between sorts). The same values as particle_to_global,
+// split into the low and high words. False: not in reach (the caller goes global).
+template <int S, bool QC>
+__device__ __noinline__ bool stale_to_tile(const DepArgs& a, uint32_t key, float rx, float ry, float qn, int x0, int y0,
+                                           int tw, int th, int SW, uint32_t* slo, int* shi) {
+    constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, NV = NX * NX;
+    static_assert(S != S_ESK, "trajectory frames stay on the global path");
+    if (key >= (uint32_t)a.Nx * (uint32_t)a.Ny) return false;
+    const int iy = (int)(key / (uint32_t)a.Nx), ix = (int)(key - (uint32_t)iy * (uint32_t)a.Nx);
+    int cx = ix - x0, cy = iy - y0;
+    // the periodic image nearest the tile (any image maps back to the same node)
+    if (cx > a.Nx / 2) cx -= a.Nx;
+    if (cx < -(a.Nx / 2)) cx += a.Nx;
+    if (cy > a.Ny / 2) cy -= a.Ny;
+    if (cy < -(a.Ny / 2)) cy += a.Ny;
+    if (cx < -1 || cx > tw || cy < -1 || cy > th) return false;
+    const int lx0 = cx + 2 + LO, ly0 = cy + 2 + LO;  // local node of frame entry (0, 0)
+    long long tv[NV];
+    if constexpr (S == S_TSC && QC) {
+        uint32_t X[4], Y[4];
+        tsci_weights(rx, ry, X, Y);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) tv[j * 4 + i] = (long long)((unsigned long long)X[i] * Y[j]);
+    } else if constexpr (S == S_TSC) {
+        uint32_t val[16];
+        tsc_values(rx, ry, qn, val);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) tv[q] = tsc_true(q, val[q], 1u);
+    } else {
+        int iv[Frame<S>::V];
+        stencil_values<S>(a, rx, ry, qn, 0.0f, 0.0f, ix, iy, 0, iv);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) tv[q] = iv[q];
+    }
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        const long long x = tv[q];
+        if (x != 0) {
+            const int i = (ly0 + q / NX) * SW + lx0 + (q % NX);
+            atomicAdd(slo + i, (uint32_t)x & ((1u << TILE_SPLIT) - 1u));
+            atomicAdd(shi + i, (int)(x >> TILE_SPLIT));
+        }
+    }
+    return true;
+}
+
 // Shared memory: [stage buffers: NW warps x NBUF x NF fields x LPP/4 quads x
 // 32 lanes x 16 bytes][tile accumulators: low, high words][the tile rows' cell
 // offsets].
@@ -1159,11 +1210,14 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint32_t s_count;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int SW = a.tile_w + 3;
+    // between sorts the accumulators get one more halo cell on each side, where
+    // the particles that moved to a neighbouring cell of the tile land
+    constexpr int PAD = (KEYS && S != S_ESK) ? 1 : 0;
+    const int SW = a.tile_w + 3 + 2 * PAD;
     const int tx = blockIdx.x % a.tiles_x, ty = blockIdx.x / a.tiles_x;
     const int x0 = tx * a.tile_w, y0 = ty * a.tile_h;
     const int tw = min(a.tile_w, a.Nx - x0), th = min(a.tile_h, a.Ny - y0);
-    const int nloc = (th + 3) * SW;
+    const int nloc = (th + 3 + 2 * PAD) * SW;
     const int nch = (tw + 31) >> 5;  // units of up to 32 cells per tile row
     unsigned char* swarp = smem_raw + (size_t)warp * NBUF * BUFB;
     const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(swarp) + (uint32_t)(lane * 16);
@@ -1344,7 +1398,12 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
                         vxx = a.vx[p];
                         vyy = a.vy[p];
                     }
-                    stale_to_global<S, QC>(a, a.cell[p], a.xr[p], a.yr[p], QC ? a.qc : a.q[p], vxx, vyy, p);
+                    const uint32_t key = a.cell[p];
+                    const float rx = a.xr[p], ry = a.yr[p], qn = QC ? a.qc : a.q[p];
+                    if constexpr (PAD > 0) {
+                        if (!dense && stale_to_tile<S, QC>(a, key, rx, ry, qn, x0, y0, tw, th, SW, slo, shi)) continue;
+                    }
+                    stale_to_global<S, QC>(a, key, rx, ry, qn, vxx, vyy, p);
                 }
                 __syncwarp();
             }
@@ -1359,8 +1418,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
                 if (dense) {
                     flush_global_ll<NX, LO, NV>(a, mykey, tv);
                 } else {
-                    const int lx = cw.col + 1 + LO;
-                    const int lrow = cw.r + 1 + LO;
+                    const int lx = cw.col + 1 + LO + PAD;
+                    const int lrow = cw.r + 1 + LO + PAD;
 #pragma unroll
                     for (int q = 0; q < NV; ++q) {
                         const long long x = tv[q];
@@ -1396,7 +1455,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
         const long long v = hi * (1ll << TILE_SPLIT) + (long long)slo[i];
         if (v != 0) {
             const int ly = i / SW, lx = i % SW;
-            const int gx = wrap_i(x0 - 1 + lx, a.Nx), gy = wrap_i(y0 - 1 + ly, a.Ny);
+            const int gx = wrap_i(x0 - 1 - PAD + lx, a.Nx), gy = wrap_i(y0 - 1 - PAD + ly, a.Ny);
             atomicAdd(a.acc + (size_t)gy * a.Nx + gx, (unsigned long long)v);
         }
     }
@@ -1425,8 +1484,9 @@ __global__ void fixed_to_rho(const long long* __restrict__ acc, size_t g, double
 template <int S, int LPP, int NW, int MINB, bool QC, bool KEYS>
 static int launch_cells(pic_ctx* c, const DepArgs& a, unsigned tiles) {
     constexpr int NBUF = CELLS_NBUF;
+    constexpr int PAD = (KEYS && S != S_ESK) ? 1 : 0;  // the kernel's extra halo between sorts
     const size_t smem = cells_fixed_bytes<S, LPP, NW, QC, KEYS, NBUF>() +
-                        (size_t)(a.tile_h + 3) * (a.tile_w + 3) * 2 * sizeof(uint32_t) +
+                        (size_t)(a.tile_h + 3 + 2 * PAD) * (a.tile_w + 3 + 2 * PAD) * 2 * sizeof(uint32_t) +
                         (size_t)a.tile_h * (a.tile_w + 1) * sizeof(uint32_t) +
                         (KEYS ? (size_t)NW * 32 * LPP * sizeof(uint32_t) : 0);
     const int rc = opt_in_dynamic_smem((const void*)deposit_cells<S, LPP, NW, MINB, QC, KEYS, NBUF>, smem);
