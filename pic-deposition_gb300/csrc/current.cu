@@ -21,10 +21,11 @@
 // quantities of their own size (no S1 - S0 cancellation): no crossing
 // DS = (0,-d,d,0); crossing up DS = (0, r-1, (1-r)-fr, fr); down DS = (-e, r+e, -r, 0).
 //
-// Kernel: the deposit's warp step (128 particles, 4 consecutive per lane via
-// 128-bit loads), each lane summing its particles' 24 edge values while they
-// share a cell (one rolled copy of the particle body), a segmented warp scan,
-// and int64 atomics from the run tails.
+// Kernels: cell-sorted particles, one lane per cell (current_cells); any order,
+// the deposit's warp step (128 particles, 4 consecutive per lane via 128-bit
+// loads), each lane summing its particles' 24 edge values while they share a
+// cell (one rolled copy of the particle body), a segmented warp scan, and int64
+// atomics from the run tails (deposit_current).
 #include "pic_internal.cuh"
 
 namespace picgb {
@@ -256,6 +257,97 @@ __global__ void __launch_bounds__(J_THREADS) deposit_current(JArgs a) {
     }
 }
 
+// Cell-sorted particles: one lane per cell. A CTA owns a 32 x 8 tile of cells;
+// warp w takes the tile rows w, w + 4, and lane l the cell in column l, walking
+// that cell's range of the sorted stream (16-byte loads of 4 particles) and
+// summing its particles' 24 edge values in 32-bit registers (at most 64
+// particles per sum: |sum| <= 64 * 2^24). Each sum goes to the tile's Jx and Jy
+// accumulators in shared memory (low 15 bits and the rest in two 32-bit words,
+// a halo of one node left and below and two right and above), and the tile to
+// the int64 grids once. Integer sums, so the grids equal those of
+// deposit_current bit for bit.
+constexpr int JC_TW = 32, JC_TH = 8, JC_WARPS = 4;
+constexpr int JC_SW = JC_TW + 3, JC_SH = JC_TH + 3, JC_N = JC_SW * JC_SH;
+constexpr int JC_RUN = 64;
+constexpr int JC_SPLIT = 15;
+
+template <bool QC>
+__global__ void __launch_bounds__(JC_WARPS * 32) current_cells(JArgs a, const uint32_t* __restrict__ offsets,
+                                                                int tiles_x) {
+    __shared__ uint32_t slo[2 * JC_N];
+    __shared__ int shi[2 * JC_N];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    const int x0 = tx * JC_TW, y0 = ty * JC_TH;
+    const int tw = min(JC_TW, a.Nx - x0), th = min(JC_TH, a.Ny - y0);
+    for (int i = threadIdx.x; i < 2 * JC_N; i += JC_WARPS * 32) {
+        slo[i] = 0;
+        shi[i] = 0;
+    }
+    __syncthreads();
+    int acc[NJ];
+    // adds acc (the cell in column `lane`, tile row r) to the tile accumulators
+    auto flush = [&](int r) {
+#pragma unroll
+        for (int t = 0; t < NJ; ++t) {
+            const int v = acc[t];
+            if (v != 0) {
+                // Jx edge (j, i) = t (j * 3 + i), Jy edge (j, i) = t - 12 (j * 4 + i): local node (lane + i, r + j)
+                const int j = t < 12 ? t / 3 : (t - 12) / 4, i = t < 12 ? t % 3 : (t - 12) % 4;
+                const int idx = (t < 12 ? 0 : JC_N) + (r + j) * JC_SW + lane + i;
+                atomicAdd(slo + idx, (uint32_t)v & ((1u << JC_SPLIT) - 1u));
+                atomicAdd(shi + idx, v >> JC_SPLIT);
+            }
+            acc[t] = 0;
+        }
+    };
+    for (int r = warp; r < th; r += JC_WARPS) {
+        uint32_t beg = 0, end = 0;
+        if (lane < tw) {
+            const uint32_t cell = (uint32_t)(y0 + r) * (uint32_t)a.Nx + (uint32_t)(x0 + lane);
+            beg = offsets[cell];
+            end = offsets[cell + 1];
+        }
+#pragma unroll
+        for (int t = 0; t < NJ; ++t) acc[t] = 0;
+        int cnt = 0;
+        const uint32_t q0 = beg >> 2, q1 = end > beg ? (end + 3u) >> 2 : q0;
+#pragma unroll 1
+        for (uint32_t qd = q0; qd < q1; ++qd) {
+            const float4 xr = __ldg(reinterpret_cast<const float4*>(a.xr) + qd);
+            const float4 yr = __ldg(reinterpret_cast<const float4*>(a.yr) + qd);
+            const float4 vx = __ldg(reinterpret_cast<const float4*>(a.vx) + qd);
+            const float4 vy = __ldg(reinterpret_cast<const float4*>(a.vy) + qd);
+            const float4 q = QC ? make_float4(a.qc, a.qc, a.qc, a.qc) : __ldg(reinterpret_cast<const float4*>(a.q) + qd);
+#pragma unroll 1
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t p = 4u * qd + (uint32_t)k;
+                if (p < beg || p >= end) continue;
+                int v[NJ];
+                if (edge_values(a, f4(xr, k), f4(yr, k), f4(vx, k), f4(vy, k), f4(q, k), p, v)) {
+#pragma unroll
+                    for (int t = 0; t < NJ; ++t) acc[t] += v[t];
+                }
+                if (++cnt == JC_RUN) {
+                    flush(r);
+                    cnt = 0;
+                }
+            }
+        }
+        if (cnt) flush(r);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 2 * JC_N; i += JC_WARPS * 32) {
+        const long long v = (long long)shi[i] * (1ll << JC_SPLIT) + (long long)slo[i];
+        if (v != 0) {
+            const int li = i < JC_N ? i : i - JC_N;
+            const int ly = li / JC_SW, lx = li - ly * JC_SW;
+            const size_t g = (size_t)wrap_i(y0 - 1 + ly, a.Ny) * a.Nx + wrap_i(x0 - 1 + lx, a.Nx);
+            atomicAdd((i < JC_N ? a.jx : a.jy) + g, (unsigned long long)v);
+        }
+    }
+}
+
 __global__ void current_to_f64(const long long* __restrict__ jx, const long long* __restrict__ jy, size_t g,
                                const double* __restrict__ units, double* __restrict__ ox, double* __restrict__ oy) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -306,7 +398,17 @@ int deposit_current_async(pic_ctx* c, double dt) {
     a.jx = reinterpret_cast<unsigned long long*>(c->accjx);
     a.jy = reinterpret_cast<unsigned long long*>(c->accjy);
     a.st = c->dstats;
-    if (c->n) {
+    if (c->n && c->sorted) {
+        // cell-sorted: one lane per cell over the sort's ranges
+        const int tiles_x = (c->Nx + JC_TW - 1) / JC_TW, tiles_y = (c->Ny + JC_TH - 1) / JC_TH;
+        prof_begin(c, "current");
+        if (a.qc != 0.0f)
+            current_cells<true><<<(unsigned)(tiles_x * tiles_y), JC_WARPS * 32, 0, c->stream>>>(a, c->offsets, tiles_x);
+        else
+            current_cells<false><<<(unsigned)(tiles_x * tiles_y), JC_WARPS * 32, 0, c->stream>>>(a, c->offsets, tiles_x);
+        prof_end(c);
+        PIC_TRY(check_launch(c, "current_cells"));
+    } else if (c->n) {
         int sms = 148;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
         size_t blocks = (c->n + J_THREADS * 4 - 1) / (J_THREADS * 4);

@@ -77,14 +77,19 @@ def test_current_config2_shape_slice(pg, port):
     assert np.linalg.norm(jy_f - rjy) / np.linalg.norm(rjy) <= REL_L2_TOL
 
 
-def test_courant_violation_is_an_error(pg, port):
+@pytest.mark.parametrize("sort", [False, True])
+def test_courant_violation_is_an_error(pg, port, sort):
     p = port.init_particles(0, 16, 16, 16.0, 16.0, 1000, p0=1.0, seed=1)
     p["vx"][7] = 50.0
     with pg.Context(16, 16, 16.0, 16.0, 1000) as c:
         c.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+        if sort:
+            c.sort()
         with pytest.raises(pg.PicError) as e:
             c.deposit_current(0.1)
         assert e.value.code == -6
         p["vx"][7] = 0.0
         c.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+        if sort:
+            c.sort()
         c.deposit_current(0.1)  # context still usable
