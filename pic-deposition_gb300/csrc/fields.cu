@@ -122,9 +122,9 @@ __global__ void __launch_bounds__(RED_THREADS) sum_v2_partials(const float* __re
 }
 
 __global__ void __launch_bounds__(RED_THREADS) sum_final(const double* __restrict__ partial, double scale,
-                                                        double* out) {
+                                                        double* out, int count = RED_BLOCKS) {
     double s = 0.0;
-    for (int i = threadIdx.x; i < RED_BLOCKS; i += RED_THREADS) s = __dadd_rn(s, partial[i]);
+    for (int i = threadIdx.x; i < count; i += RED_THREADS) s = __dadd_rn(s, partial[i]);
     const double t = block_sum(s);
     if (threadIdx.x == 0) *out = __dmul_rn(t, scale);
 }
@@ -240,6 +240,7 @@ int ensure_fields(pic_ctx* c) {
     if (!c->Eyf) c->Eyf = (float*)dalloc(g * 4, &rc);
     if (rc) return rc;
     if (!c->red_partials) c->red_partials = (double*)dalloc(RED_BLOCKS * 8, &rc);
+    if (!rc && !c->ke_partials) c->ke_partials = (double*)dalloc(MOVE_KE_BLOCKS * 8, &rc);
     if (rc) return rc;
     if (!c->red_out) c->red_out = (double*)dalloc(16 * 8, &rc);
     if (rc) return rc;
@@ -280,7 +281,8 @@ void release_fields(pic_ctx* c) {
         cufftDestroy((cufftHandle)c->fft_inv);
         c->fft_ready = 0;
     }
-    void* ptrs[] = {c->phi, c->Ex, c->Ey, c->Exf, c->Eyf, c->spec, c->fft_rhs, c->red_partials, c->red_out};
+    void* ptrs[] = {c->phi, c->Ex, c->Ey, c->Exf, c->Eyf, c->spec, c->fft_rhs, c->red_partials, c->red_out,
+                    c->ke_partials};
     for (void* p : ptrs) dfree(p);
 }
 
@@ -368,6 +370,10 @@ int diagnostics_async(pic_ctx* c) {
     if (a.m) {
         a.kind = SUM_KE;
         PIC_TRY(device_sum(c, a, c->red_out + 3));
+    } else if (c->n > 0 && c->ke_ready) {  // left by the gather that produced these velocities
+        c->ke_ready = 0;                     // used once: the next diagnostics recompute unless a gather refills it
+        sum_final<<<1, RED_THREADS, 0, c->stream>>>(c->ke_partials, 0.5, c->red_out + 3, MOVE_KE_BLOCKS);
+        PIC_TRY(check_launch(c, "sum_final"));
     } else if (c->n > 0) {
         sum_v2_partials<<<RED_BLOCKS, RED_THREADS, 0, c->stream>>>(c->vx, c->vy, c->n, c->red_partials);
         PIC_TRY(check_launch(c, "sum_v2_partials"));

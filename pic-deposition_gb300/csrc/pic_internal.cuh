@@ -39,6 +39,7 @@ enum DevErr : int {
 // the sorted deposit reads four consecutive particles with one 128-bit load
 // from a 4-aligned index below n, which may reach up to 3 elements past n.
 constexpr size_t PARTICLE_PAD = 32;
+constexpr int MOVE_KE_BLOCKS = 4096;  // fixed grid of a gather that sums the kinetic energy
 
 struct WsState;
 
@@ -106,6 +107,10 @@ struct pic_ctx {
     // deterministic FP64 reductions
     double* red_partials = nullptr;
     double* red_out = nullptr;
+    // per-block sums of vx^2 + vy^2 left by a time step's gather (MOVE_KE_BLOCKS
+    // entries); ke_ready: they belong to the current velocities
+    double* ke_partials = nullptr;
+    int ke_ready = 0;
     // red_out[8], red_out[9] hold sum(q) and sum(|q|) of the current particle set:
     // charges do not change while particles move or are sorted
     int qsum_valid = 0;

@@ -22,6 +22,7 @@
 namespace picgb {
 
 struct MoveArgs {
+    double* ke_partial;  // KE: per-block sums of vx^2 + vy^2 after the gather
     uint32_t* cell;
     float *xr, *yr, *vx, *vy;
     const float* q;
@@ -49,8 +50,23 @@ __device__ __forceinline__ void drift(float& r, int& i, float v, float dtd, int 
     i = wrap_near(i + (int)s, n);
 }
 
-template <bool GATHER, bool PUSH>
+// Running double-FP32 sum (Knuth's two-sum): fields.cu's kinetic sum, per thread.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float t) {
+    const float s = __fadd_rn(hi, t);
+    const float v = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, v)), __fsub_rn(t, v));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+
+// KE (with GATHER, every mass 1): the sum of vx^2 + vy^2 of the updated
+// velocities in the arithmetic of fields.cu's sum_v2_partials (exact FP32
+// squares, double-FP32 per thread, FP64 across the block in a fixed order),
+// one partial per block of a fixed grid: the time step's kinetic energy
+// without another pass over the velocities.
+template <bool GATHER, bool PUSH, bool KE = false>
 __global__ void __launch_bounds__(256) move_particles(MoveArgs a) {
+    float ke_hi = 0.0f, ke_lo = 0.0f;
     const float maxq = load_maxq(a.st);
     const float inv_nx = 1.0f / (float)a.Nx;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -91,6 +107,13 @@ __global__ void __launch_bounds__(256) move_particles(MoveArgs a) {
             vyy = vyy + (coef * ey) * a.dtf;
             a.vx[p] = vxx;
             a.vy[p] = vyy;
+            if constexpr (KE) {
+                const float px = __fmul_rn(vxx, vxx), py = __fmul_rn(vyy, vyy);
+                const float ex2 = __fmaf_rn(vxx, vxx, -px), ey2 = __fmaf_rn(vyy, vyy, -py);
+                two_sum_acc(ke_hi, ke_lo, px);
+                two_sum_acc(ke_hi, ke_lo, py);
+                ke_lo = __fadd_rn(ke_lo, __fadd_rn(ex2, ey2));
+            }
         }
         if constexpr (PUSH) {
             drift(rx, ix, vxx, a.dtdx, a.Nx);
@@ -105,12 +128,30 @@ __global__ void __launch_bounds__(256) move_particles(MoveArgs a) {
         vxx = nvx;
         vyy = nvy;
     }
+    if constexpr (KE) {
+        __shared__ double ws[8];
+        double v = __dadd_rn((double)ke_hi, (double)ke_lo);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
+        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < 8; ++w) t = __dadd_rn(t, ws[w]);
+            a.ke_partial[blockIdx.x] = t;
+        }
+    }
 }
 
-int move(pic_ctx* c, double dt, bool gather, bool push) {
+// ke: with the gather and unit masses, also leave the kinetic sums of the
+// updated velocities in c->ke_partials (fixed grid of MOVE_KE_BLOCKS blocks).
+int move(pic_ctx* c, double dt, bool gather, bool push, bool ke) {
+    c->ke_ready = 0;
     if (c->n == 0) return PIC_OK;
     if (gather) PIC_TRY(ensure_fields(c));
+    ke = ke && gather && !c->has_mass;
     MoveArgs a;
+    a.ke_partial = c->ke_partials;
     a.cell = c->cell;
     a.xr = c->xr;
     a.yr = c->yr;
@@ -132,18 +173,24 @@ int move(pic_ctx* c, double dt, bool gather, bool push) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     size_t blocks = (c->n + 255) / 256;
     if (blocks > (size_t)sms * 32) blocks = (size_t)sms * 32;
+    if (ke) blocks = MOVE_KE_BLOCKS;  // the partition of the sums does not depend on the device
     prof_begin(c, gather && push ? "gather_push" : gather ? "gather" : "push");
     if (gather && push)
-        move_particles<true, true><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+        ke ? move_particles<true, true, true><<<(unsigned)blocks, 256, 0, c->stream>>>(a)
+           : move_particles<true, true><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
     else if (gather)
-        move_particles<true, false><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+        ke ? move_particles<true, false, true><<<(unsigned)blocks, 256, 0, c->stream>>>(a)
+           : move_particles<true, false><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
     else
         move_particles<false, true><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
     prof_end(c);
     PIC_TRY(check_launch(c, "move_particles"));
     if (push) c->sorted = 0;
+    c->ke_ready = ke ? 1 : 0;
     return PIC_OK;
 }
+
+int move(pic_ctx* c, double dt, bool gather, bool push) { return move(c, dt, gather, push, false); }
 
 }  // namespace picgb
 

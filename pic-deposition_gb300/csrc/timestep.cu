@@ -27,6 +27,7 @@
 namespace picgb {
 
 int move(pic_ctx* c, double dt, bool gather, bool push);
+int move(pic_ctx* c, double dt, bool gather, bool push, bool ke);
 int rbgs_solve_async(pic_ctx* c, double tol, int max_iters, int check_every);
 int ws_warm_guess(pic_ctx* c, int mode);
 int ws_record_solution(pic_ctx* c);
@@ -93,11 +94,11 @@ static int one_step(pic_ctx* c, const pic_run_config* cfg, bool do_sort, double*
         PIC_TRY(count_moved());
         PIC_TRY(solve(c, cfg));
         PIC_TRY(move(c, cfg->dt, false, true));
-        PIC_TRY(move(c, cfg->dt, true, false));
+        PIC_TRY(move(c, cfg->dt, true, false, true));
         return record_step(c, hist, step_ctr, steps);
     }
     if (head) {
-        PIC_TRY(move(c, cfg->dt, true, true));
+        PIC_TRY(move(c, cfg->dt, true, true, true));
         PIC_TRY(record_step(c, hist, step_ctr, steps));
     } else {
         PIC_TRY(move(c, cfg->dt, false, true));
@@ -292,7 +293,7 @@ int run_steps(pic_ctx* c, const pic_run_config* cfg, int steps, pic_diag* histor
             PIC_TRY(after_step());
         }
         if (!esk) {  // the last step's gather and diagnostics
-            PIC_TRY(move(c, cfg->dt, true, false));
+            PIC_TRY(move(c, cfg->dt, true, false, true));
             PIC_TRY(record_step(c, hist, ctr, steps));
         }
         if (history)
