@@ -797,7 +797,7 @@ def run_config3(args):
     background 1/V), TSC, cell sort every 10 steps, FFT Poisson, fused graph steps."""
     import pic_gb300 as pg
 
-    N, ppc = 2048, 100
+    N, ppc = args.c3_n, 100
     n = N * N * ppc
     steps, dt = args.c3_steps, 0.1
     out = {"workload": f"timestep_twostream_tsc_{N}x{N}_{ppc}ppc", "particles": n, "steps": steps, "dt": dt,
@@ -887,6 +887,7 @@ def main():
     ap.add_argument("--c3-only", action="store_true", help="only the 2048^2 two-stream time step")
     ap.add_argument("--no-c3", action="store_true", help="skip the 2048^2 two-stream time step")
     ap.add_argument("--c3-steps", type=int, default=2000)
+    ap.add_argument("--c3-n", type=int, default=2048, help="grid N x N of the two-stream time step (2048 = the workload)")
     ap.add_argument("--nn-only", action="store_true", help="only the convolution-kernel throughput")
     ap.add_argument("--nn-batch", type=int, default=8)
     ap.add_argument("--nn-reps", type=int, default=5)
