@@ -91,16 +91,9 @@ __global__ void __launch_bounds__(RED_THREADS) sum_partials(SumArgs a, double* _
 // Sum of vx^2 + vy^2 over the particles with no FP64 arithmetic per particle
 // (FP64 is slow on this part): each square is formed exactly as an FP32 pair
 // (product and its fused-multiply-add error), each thread accumulates in
-// double-FP32 (Knuth's two-sum keeps the running sum's rounding errors), and the
-// threads' totals enter the same deterministic FP64 block and grid sums. Agrees
-// with an FP64 sum of the squares to about 1e-14 relative.
-__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float t) {
-    const float s = __fadd_rn(hi, t);
-    const float v = __fsub_rn(s, hi);
-    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, v)), __fsub_rn(t, v));
-    hi = s;
-    lo = __fadd_rn(lo, err);
-}
+// double-FP32 (Knuth's two-sum keeps the running sum's rounding errors; ke_add),
+// and the threads' totals enter the same deterministic FP64 block and grid sums.
+// Agrees with an FP64 sum of the squares to about 1e-14 relative.
 
 __global__ void __launch_bounds__(RED_THREADS) sum_v2_partials(const float* __restrict__ vx,
                                                               const float* __restrict__ vy, size_t n,
@@ -110,12 +103,7 @@ __global__ void __launch_bounds__(RED_THREADS) sum_v2_partials(const float* __re
     const size_t e = b + chunk < n ? b + chunk : n;
     float hi = 0.0f, lo = 0.0f;
     for (size_t i = b + threadIdx.x; i < e; i += RED_THREADS) {
-        const float x = vx[i], y = vy[i];
-        const float px = __fmul_rn(x, x), py = __fmul_rn(y, y);
-        const float ex = __fmaf_rn(x, x, -px), ey = __fmaf_rn(y, y, -py);
-        two_sum_acc(hi, lo, px);
-        two_sum_acc(hi, lo, py);
-        lo = __fadd_rn(lo, __fadd_rn(ex, ey));
+        ke_add(hi, lo, vx[i], vy[i]);
     }
     const double t = block_sum(__dadd_rn((double)hi, (double)lo));
     if (threadIdx.x == 0) partial[blockIdx.x] = t;
@@ -372,7 +360,7 @@ int diagnostics_async(pic_ctx* c) {
         PIC_TRY(device_sum(c, a, c->red_out + 3));
     } else if (c->n > 0 && c->ke_ready) {  // left by the gather that produced these velocities
         c->ke_ready = 0;                     // used once: the next diagnostics recompute unless a gather refills it
-        sum_final<<<1, RED_THREADS, 0, c->stream>>>(c->ke_partials, 0.5, c->red_out + 3, MOVE_KE_BLOCKS);
+        sum_final<<<1, RED_THREADS, 0, c->stream>>>(c->ke_partials, 0.5, c->red_out + 3, c->ke_count);
         PIC_TRY(check_launch(c, "sum_final"));
     } else if (c->n > 0) {
         sum_v2_partials<<<RED_BLOCKS, RED_THREADS, 0, c->stream>>>(c->vx, c->vy, c->n, c->red_partials);

@@ -111,6 +111,7 @@ struct pic_ctx {
     // entries); ke_ready: they belong to the current velocities
     double* ke_partials = nullptr;
     int ke_ready = 0;
+    int ke_count = 0;  // entries the last gather filled
     // red_out[8], red_out[9] hold sum(q) and sum(|q|) of the current particle set:
     // charges do not change while particles move or are sorted
     int qsum_valid = 0;
@@ -174,7 +175,9 @@ int exclusive_scan_u32(pic_ctx* ctx, unsigned int* data, size_t n);
 int ensure_sort_scratch(pic_ctx* ctx);
 // Per-cell offsets of cell-ordered keys (histogram + scan into ctx->offsets).
 int build_offsets(pic_ctx* ctx, const uint32_t* keys);
-int sort_particles(pic_ctx* ctx);
+// perm: also build the permutation (idx_a) that pic_gpu_sort returns; the
+// library's own sorts (time step, ensemble, warm start) do not read it
+int sort_particles(pic_ctx* ctx, bool perm = false);
 
 // Fields, Poisson and diagnostics (fields.cu).
 int ensure_fields(pic_ctx* ctx);
@@ -268,6 +271,43 @@ __device__ __forceinline__ void set_dev_error(DevStats* st, int code, unsigned i
 }
 
 __device__ __forceinline__ float load_maxq(const DevStats* st) { return __uint_as_float(st->maxq_bits); }
+
+// CIC interpolation of a node field at cell offsets (wx, wy), in the
+// reference's operation order (deposition.cpp:335-356); the build uses
+// --fmad=false, so the oracle reproduces every bit.
+__device__ __forceinline__ float interp_nodes(float e00, float e10, float e01, float e11, float wx, float wy) {
+    const float omx = 1.0f - wx, omy = 1.0f - wy;
+    return (((e00 * omx) * omy + (e10 * wx) * omy) + (e01 * omx) * wy) + (e11 * wx) * wy;
+}
+__device__ __forceinline__ float interp(const float* __restrict__ E, size_t i00, size_t i10, size_t i01, size_t i11,
+                                        float wx, float wy) {
+    return interp_nodes(__ldg(E + i00), __ldg(E + i10), __ldg(E + i01), __ldg(E + i11), wx, wy);
+}
+
+// x += v*dt/dx in cell-relative form: the integer part moves the cell index (wrapped).
+__device__ __forceinline__ void drift(float& r, int& i, float v, float dtd, int n) {
+    const float x = r + v * dtd;
+    const float s = floorf(x);
+    r = x - s;
+    i = wrap_near(i + (int)s, n);
+}
+
+// Running double-FP32 sum (Knuth's two-sum) of the kinetic-energy partials.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float t) {
+    const float s = __fadd_rn(hi, t);
+    const float v = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, v)), __fsub_rn(t, v));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+// Adds vx^2 + vy^2 to a double-FP32 sum: exact FP32 squares (product and FMA error).
+__device__ __forceinline__ void ke_add(float& hi, float& lo, float vx, float vy) {
+    const float px = __fmul_rn(vx, vx), py = __fmul_rn(vy, vy);
+    const float ex = __fmaf_rn(vx, vx, -px), ey = __fmaf_rn(vy, vy, -py);
+    two_sum_acc(hi, lo, px);
+    two_sum_acc(hi, lo, py);
+    lo = __fadd_rn(lo, __fadd_rn(ex, ey));
+}
 
 // Domain::cellCoords (src/pic/domain.hpp:34-43) in FP64: w = x/dx, i = floor(w),
 // frac = w - i, i wrapped. When dx is a power of two, x * (1/dx) equals the

@@ -36,28 +36,6 @@ struct MoveArgs {
     const DevStats* st;
 };
 
-__device__ __forceinline__ float interp(const float* __restrict__ E, size_t i00, size_t i10, size_t i01, size_t i11,
-                                        float wx, float wy) {
-    const float omx = 1.0f - wx, omy = 1.0f - wy;
-    return (((__ldg(E + i00) * omx) * omy + (__ldg(E + i10) * wx) * omy) + (__ldg(E + i01) * omx) * wy) +
-           (__ldg(E + i11) * wx) * wy;
-}
-
-__device__ __forceinline__ void drift(float& r, int& i, float v, float dtd, int n) {
-    const float x = r + v * dtd;
-    const float s = floorf(x);
-    r = x - s;
-    i = wrap_near(i + (int)s, n);
-}
-
-// Running double-FP32 sum (Knuth's two-sum): fields.cu's kinetic sum, per thread.
-__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float t) {
-    const float s = __fadd_rn(hi, t);
-    const float v = __fsub_rn(s, hi);
-    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, v)), __fsub_rn(t, v));
-    hi = s;
-    lo = __fadd_rn(lo, err);
-}
 
 // KE (with GATHER, every mass 1): the sum of vx^2 + vy^2 of the updated
 // velocities in the arithmetic of fields.cu's sum_v2_partials (exact FP32
@@ -107,13 +85,7 @@ __global__ void __launch_bounds__(256) move_particles(MoveArgs a) {
             vyy = vyy + (coef * ey) * a.dtf;
             a.vx[p] = vxx;
             a.vy[p] = vyy;
-            if constexpr (KE) {
-                const float px = __fmul_rn(vxx, vxx), py = __fmul_rn(vyy, vyy);
-                const float ex2 = __fmaf_rn(vxx, vxx, -px), ey2 = __fmaf_rn(vyy, vyy, -py);
-                two_sum_acc(ke_hi, ke_lo, px);
-                two_sum_acc(ke_hi, ke_lo, py);
-                ke_lo = __fadd_rn(ke_lo, __fadd_rn(ex2, ey2));
-            }
+            if constexpr (KE) ke_add(ke_hi, ke_lo, vxx, vyy);
         }
         if constexpr (PUSH) {
             drift(rx, ix, vxx, a.dtdx, a.Nx);
@@ -187,6 +159,7 @@ int move(pic_ctx* c, double dt, bool gather, bool push, bool ke) {
     PIC_TRY(check_launch(c, "move_particles"));
     if (push) c->sorted = 0;
     c->ke_ready = ke ? 1 : 0;
+    c->ke_count = MOVE_KE_BLOCKS;
     return PIC_OK;
 }
 

@@ -290,7 +290,7 @@ static int launch_pass(pic_ctx* c, const uint32_t* kin, uint32_t* kout, size_t n
     return check_launch(c, "radix_scatter");
 }
 
-int sort_particles(pic_ctx* c) {
+int sort_particles(pic_ctx* c, bool perm) {
     PIC_TRY(ensure_sort_scratch(c));
     const size_t n = c->n;
     if (n == 0) {
@@ -302,8 +302,10 @@ int sort_particles(pic_ctx* c) {
     int bits = 0;
     while (bits < 32 && ((c->G - 1) >> bits) != 0) ++bits;
     if (bits == 0) {  // one cell: already in order; the permutation is the identity
-        iota_u32<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->idx_a, n);
-        PIC_TRY(check_launch(c, "iota_u32"));
+        if (perm) {
+            iota_u32<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->idx_a, n);
+            PIC_TRY(check_launch(c, "iota_u32"));
+        }
         PIC_TRY(build_offsets(c, c->cell));
         c->sorted = 1;
         c->part_valid = 1;
@@ -312,7 +314,8 @@ int sort_particles(pic_ctx* c) {
     const int passes = (bits + RS_MAX_BITS - 1) / RS_MAX_BITS;
     const int width = (bits + passes - 1) / passes;
     // the payload: offsets, velocities, charges (not when uniform: any order of
-    // equal values is the same array), masses (when stored) and the permutation
+    // equal values is the same array), masses (when stored) and, when asked for,
+    // the permutation
     float** slots[6] = {&c->xr, &c->yr, &c->vx, &c->vy, &c->q, &c->m};
     int fields[6], nf = 0;
     for (int k = 0; k < 6; ++k)
@@ -321,13 +324,15 @@ int sort_particles(pic_ctx* c) {
         const int w = (bits - shift) < width ? (bits - shift) : width;
         const uint32_t mask = (1u << w) - 1u;
         Payload pay;
-        pay.count = nf + 1;
+        pay.count = nf + (perm ? 1 : 0);
         for (int j = 0; j < nf; ++j) {
             pay.src[j] = reinterpret_cast<const uint32_t*>(*slots[fields[j]]);
             pay.dst[j] = reinterpret_cast<uint32_t*>(c->alt[fields[j]]);
         }
-        pay.src[nf] = pass == 0 ? nullptr : c->idx_a;  // the first pass starts from the identity
-        pay.dst[nf] = c->idx_b;
+        if (perm) {
+            pay.src[nf] = pass == 0 ? nullptr : c->idx_a;  // the first pass starts from the identity
+            pay.dst[nf] = c->idx_b;
+        }
         int rc;
         if (width <= 8)
             rc = launch_pass<8>(c, c->cell, c->cell_alt, n, shift, mask, tiles, pay);
@@ -337,7 +342,7 @@ int sort_particles(pic_ctx* c) {
             rc = launch_pass<10>(c, c->cell, c->cell_alt, n, shift, mask, tiles, pay);
         PIC_TRY(rc);
         std::swap(c->cell, c->cell_alt);
-        std::swap(c->idx_a, c->idx_b);
+        if (perm) std::swap(c->idx_a, c->idx_b);
         for (int j = 0; j < nf; ++j) std::swap(*slots[fields[j]], c->alt[fields[j]]);
     }
     offsets_from_sorted<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->cell, n, (uint32_t)c->G, c->offsets,
@@ -356,7 +361,7 @@ extern "C" int pic_gpu_sort(pic_ctx* c, uint32_t* keys_out, uint32_t* perm_out, 
     if (!c) return fail(PIC_ERR_ARG, "NULL context");
     PIC_CUDA_TRY(cudaSetDevice(c->device));
     prof_begin(c, "sort");
-    const int rc = sort_particles(c);
+    const int rc = sort_particles(c, true);
     prof_end(c);
     PIC_TRY(rc);
     c->sorts++;
