@@ -1,7 +1,7 @@
 // 3x3 periodic convolutions as implicit GEMMs on the 5th-generation tensor cores.
 //
-// Forward / input-gradient kernel (conv3x3_kernel): one CTA of 4 warps owns a
-// 128-pixel segment of a run of image rows. The GEMM per output row is
+// Forward / input-gradient kernel (conv3x3_kernel): one CTA owns a 128-pixel
+// segment of a run of image rows. The GEMM per output row is
 //     D[128 px][cout] = sum over 9 taps of A_tap[128 px][cin] * B_tap[cin][cout]
 // with D in tensor memory (FP32), issued as tcgen05.mma kind::f16 (BF16 x BF16,
 // M = 128, N = cout, K = 16) by one thread. The input rows are staged in shared
@@ -10,18 +10,17 @@
 // (8-row core matrices of 16-byte rows, stride between row groups SBO = 128 B,
 // between the two K halves LBO = one plane) row r of A sits at r*16 bytes, so
 // the operand of tap dx is the same staged row with its start moved by
-// (dx+1)*16 bytes: im2col costs nothing. Rows y-1, y, y+1 live in a ring of 4
-// slots; while the MMAs of row y run, the CTA drains row y-1 from the other
-// TMEM buffer (bias + ReLU, or the ReLU mask of the backward pass) and stages
-// row y+2 with cp.async.
+// (dx+1)*16 bytes: im2col costs nothing. Warp-specialised: one warp stages rows
+// into a ring of 6 slots, one thread issues the MMAs of row y into one TMEM
+// buffer while four warps drain row y-1 from the other (bias + ReLU, or the
+// ReLU mask of the backward pass), handing over through mbarriers.
 //
-// Weight-gradient kernel (wgrad_kernel): D[(tap,ci)][co] = sum over pixels of
-// x[p+tap][ci] * dy[p][co], K = pixels. Per 64-pixel half row the CTA writes
-// the K-major operands explicitly (A: 9*cin rows plus one row of ones whose
-// product is the bias gradient; B: dy transposed) into one of two buffers and
-// issues 3 x 4 (cin 32) MMAs while it fills the other. Each CTA accumulates its
-// share of the pixels in TMEM and writes one partial sum; reduce_wgrad adds the
-// partials in a fixed order, so gradients are identical run to run.
+// Weight-gradient kernel (wgrad_kernel): D[(dy, ci)][(dx, co)] = sum over pixels
+// of x[p + (dy, dx)][ci] * dy[p][co], K = pixels, both operands MN-major as they
+// sit in NHWC memory (see the kernel's comment); the bias gradient is one more
+// MMA per K step against an all-ones operand. Each CTA accumulates its blocks
+// of pixels in TMEM and writes one partial sum; reduce_wgrad adds the partials
+// in a fixed order, so gradients are identical run to run.
 //
 // Every wait on the tensor cores is bounded (about one second of %globaltimer);
 // on expiry the kernel records an error, skips the remaining work, frees its
@@ -58,6 +57,11 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -137,20 +141,6 @@ __host__ __device__ constexpr uint32_t tmem_cols(int n) { return n <= 32 ? 32u :
 // ---------------------------------------------------------------------------
 // forward / input gradient
 // ---------------------------------------------------------------------------
-template <int CIN>
-__device__ __forceinline__ void stage_row(const ConvLaunch& a, int b, int yraw, int x0, uint32_t slot, int tid) {
-    constexpr int PLANES = CIN / 8;
-    const int yy = ((yraw % a.H) + a.H) % a.H;
-    const uint16_t* row = a.x + ((size_t)b * a.H + yy) * (size_t)a.W * CIN;
-    for (int t = tid; t < SLOTS * PLANES; t += THREADS) {
-        const int s = t / PLANES, j = t - s * PLANES;
-        int xx = x0 - 1 + s;
-        if (xx < 0) xx += a.W;
-        if (xx >= a.W) xx -= a.W;
-        cp_async16(slot + (uint32_t)(j * PLANE + s * 16), row + (size_t)xx * CIN + j * 8);
-    }
-}
-
 template <int COUT, int EPI>
 __device__ __forceinline__ void conv_epilogue(const ConvLaunch& a, int b, int y, int x0, uint32_t taddr,
                                               const float* sbias, int warp, int lane) {
@@ -197,17 +187,32 @@ struct ConvSmem {
     static constexpr int WBYTES = 9 * CIN * COUT * 2;
     static constexpr int OFF_BIAS = WBYTES;
     static constexpr int OFF_RING = ((WBYTES + COUT * 4) + 127) / 128 * 128;
-    static constexpr int BYTES = OFF_RING + 4 * SLOT;
+    static constexpr int BYTES = OFF_RING + 6 * SLOT;
 };
 
+__device__ __forceinline__ void mbar_arrive_cta(uint32_t a) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+
+// Warp-specialised: warp 4 stages input rows into the ring (cp.async), lane 0
+// of warp 5 issues each output row's MMAs, warps 0-3 (one TMEM lane quarter
+// each) run the epilogue of the previous row from the other TMEM buffer.
+// Barriers: full[s] (32 producer arrivals: the row in slot s has landed),
+// rowfree[s] (an MMA commit: the last output row that reads slot s is done),
+// tfull[b] (an MMA commit: accumulator b holds a row), tempty[b] (128
+// epilogue arrivals: accumulator b has been read). Every wait is bounded and
+// no role waits at a CTA barrier inside the loop.
+constexpr int CONV_THREADS = 192;
+constexpr int NRING = 6;
+
 template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(THREADS) conv3x3_kernel(ConvLaunch a) {
+__global__ void __launch_bounds__(CONV_THREADS) conv3x3_kernel(ConvLaunch a) {
     using L = ConvSmem<CIN, COUT>;
     constexpr int KSTEPS = CIN / 16;
     constexpr uint32_t IDESC = idesc_bf16(128, COUT);
     constexpr uint32_t TCOLS = tmem_cols(2 * COUT);
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t full[NRING], rowfree[NRING], tfull[2], tempty[2];
     __shared__ uint32_t tmem_slot;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -216,67 +221,109 @@ __global__ void __launch_bounds__(THREADS) conv3x3_kernel(ConvLaunch a) {
     const int y_begin = blockIdx.y * a.rows_per_cta;
     const int y_end = min(a.H, y_begin + a.rows_per_cta);
     if (y_begin >= y_end) return;
+    const int nout = y_end - y_begin, nrows = nout + 2;  // output rows; staged rows y_begin-1 .. y_end
     const uint32_t s_w = smem_addr(smem);
     const uint32_t s_ring = s_w + L::OFF_RING;
     float* sbias = reinterpret_cast<float*>(smem + L::OFF_BIAS);
 
-    for (int i = tid; i < L::WBYTES / 16; i += THREADS)
+    for (int i = tid; i < L::WBYTES / 16; i += CONV_THREADS)
         cp_async16(s_w + i * 16, reinterpret_cast<const uint8_t*>(a.wimg) + (size_t)i * 16);
     if (EPI != EPI_MASK && tid < COUT) sbias[tid] = a.bias[tid];
-    for (int r = -1; r <= 1; ++r) stage_row<CIN>(a, b, y_begin + r, x0, s_ring + ((y_begin + r + 4) & 3) * L::SLOT, tid);
     cp_async_wait_all();
     fence_async_smem();
     if (tid == 0) {
-        mbar_init(smem_addr(&mbar[0]), 1);
-        mbar_init(smem_addr(&mbar[1]), 1);
+        for (int i = 0; i < NRING; ++i) {
+            mbar_init(smem_addr(&full[i]), 32);
+            mbar_init(smem_addr(&rowfree[i]), 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(smem_addr(&tfull[i]), 1);
+            mbar_init(smem_addr(&tempty[i]), 128);
+        }
     }
     if (warp == 0) tmem_alloc(smem_addr(&tmem_slot), TCOLS);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    auto slot_addr = [&](int rr) { return s_ring + (uint32_t)((rr % NRING) * L::SLOT); };
 
-    bool ok = true;
-    int i = 0;
-    for (int y = y_begin; y < y_end; ++y, ++i) {
-        if (tid == 0) {
-            tc_fence_after();
-            const uint32_t d = tmem + (uint32_t)((i & 1) * COUT);
-            int k = 0;
-#pragma unroll
-            for (int t = 0; t < 9; ++t) {
-                const int dy = t / 3 - 1, dx = t % 3 - 1;
-                const uint32_t arow = s_ring + ((y + dy + 4) & 3) * L::SLOT + (dx + 1) * 16;
-#pragma unroll
-                for (int s = 0; s < KSTEPS; ++s, ++k) {
-                    const uint64_t ad = umma_desc(arow + 2 * s * PLANE, PLANE, 128);
-                    const uint64_t bd = umma_desc(s_w + (t * L::PLANES + 2 * s) * COUT * 16, COUT * 16, 128);
-                    mma_bf16(d, ad, bd, IDESC, k > 0 ? 1u : 0u);
-                }
+    int ok = 1;
+    if (warp == 4) {
+        // producer: staged row rr (input row y_begin - 1 + rr) into slot rr % NRING
+        for (int rr = 0; rr < nrows; ++rr) {
+            if (rr >= NRING &&
+                !mbar_wait(smem_addr(&rowfree[rr % NRING]), ((rr / NRING) - 1) & 1)) {
+                ok = 0;
+                break;
             }
-            mma_commit(smem_addr(&mbar[i & 1]));
+            constexpr int PLANES = CIN / 8;
+            const int yy = (((y_begin - 1 + rr) % a.H) + a.H) % a.H;
+            const uint16_t* row = a.x + ((size_t)b * a.H + yy) * (size_t)a.W * CIN;
+            const uint32_t dst = slot_addr(rr);
+            for (int t = lane; t < SLOTS * PLANES; t += 32) {
+                const int sl = t / PLANES, j = t - sl * PLANES;
+                int xx = x0 - 1 + sl;
+                if (xx < 0) xx += a.W;
+                if (xx >= a.W) xx -= a.W;
+                cp_async16(dst + (uint32_t)(j * PLANE + sl * 16), row + (size_t)xx * CIN + j * 8);
+            }
+            cp_async_commit();
+            if (rr >= 1) {  // the previous row's copies have landed: hand it over
+                cp_async_wait_group<1>();
+                fence_async_smem();
+                mbar_arrive_cta(smem_addr(&full[(rr - 1) % NRING]));
+            }
         }
-        if (i > 0) {
-            ok = __syncthreads_and(mbar_wait(smem_addr(&mbar[(i - 1) & 1]), ((i - 1) >> 1) & 1));
-            if (!ok) break;
-            tc_fence_after();
-            conv_epilogue<COUT, EPI>(a, b, y - 1, x0, lane_base + ((i - 1) & 1) * COUT, sbias, warp, lane);
-            tc_fence_before();
-        }
-        if (y + 1 < y_end) stage_row<CIN>(a, b, y + 2, x0, s_ring + ((y + 2 + 4) & 3) * L::SLOT, tid);
-        cp_async_wait_all();
-        fence_async_smem();
-        __syncthreads();
-    }
-    if (ok) {
-        const int last = i - 1;
-        ok = __syncthreads_and(mbar_wait(smem_addr(&mbar[last & 1]), (last >> 1) & 1));
         if (ok) {
+            cp_async_wait_group<0>();
+            fence_async_smem();
+            mbar_arrive_cta(smem_addr(&full[(nrows - 1) % NRING]));
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            // MMA issuer: output row i reads staged rows i, i+1, i+2
+            for (int i = 0; i < nout && ok; ++i) {
+                for (int rr = (i == 0 ? 0 : i + 2); rr <= i + 2; ++rr)
+                    if (!mbar_wait(smem_addr(&full[rr % NRING]), (rr / NRING) & 1)) ok = 0;
+                if (ok && i >= 2 && !mbar_wait(smem_addr(&tempty[i & 1]), ((i >> 1) - 1) & 1)) ok = 0;
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)((i & 1) * COUT);
+                int k = 0;
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    const int dy = t / 3, dx = t % 3;  // staged row i + dy, pixel offset dx
+                    const uint32_t arow = slot_addr(i + dy) + dx * 16;
+#pragma unroll
+                    for (int s = 0; s < KSTEPS; ++s, ++k) {
+                        const uint64_t ad = umma_desc(arow + 2 * s * PLANE, PLANE, 128);
+                        const uint64_t bd = umma_desc(s_w + (t * L::PLANES + 2 * s) * COUT * 16, COUT * 16, 128);
+                        mma_bf16(d, ad, bd, IDESC, k > 0 ? 1u : 0u);
+                    }
+                }
+                mma_commit(smem_addr(&tfull[i & 1]));
+                mma_commit(smem_addr(&rowfree[i % NRING]));  // staged row i: its last reader
+            }
+        }
+        __syncwarp();
+    } else {
+        // epilogue warps 0-3: TMEM lanes 32*warp .. 32*warp + 31 = pixels
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int i = 0; i < nout; ++i) {
+            // the TMEM load below is warp-aligned: the warp decides together
+            if (!__all_sync(0xffffffffu, mbar_wait(smem_addr(&tfull[i & 1]), (i >> 1) & 1))) {
+                ok = 0;
+                break;
+            }
             tc_fence_after();
-            conv_epilogue<COUT, EPI>(a, b, y_end - 1, x0, lane_base + (last & 1) * COUT, sbias, warp, lane);
+            conv_epilogue<COUT, EPI>(a, b, y_begin + i, x0, lane_base + (i & 1) * COUT, sbias, warp, lane);
+            tc_fence_before();
+            mbar_arrive_cta(smem_addr(&tempty[i & 1]));
         }
     }
+    cp_async_wait_all();
+    ok = __syncthreads_and(ok);
     if (!ok && tid == 0) atomicExch(a.err, 1);
     tc_fence_before();
     __syncthreads();
@@ -330,7 +377,6 @@ struct WgSmem {
     static constexpr int BYTES = OFF_ONES + WG_ONES;
 };
 
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all_groups() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void mbar_arrive(uint32_t a) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
@@ -415,7 +461,6 @@ __global__ void __launch_bounds__(THREADS) wgrad_kernel(const __grid_constant__ 
     using L = WgSmem<CIN, COUT>;
     constexpr uint32_t IDESC = idesc_bf16_mn(128, COUT);
     constexpr uint32_t TCOLS = tmem_cols(4 * COUT);
-    constexpr int XP = CIN / 8, DP = COUT / 8;
     constexpr int MPAD = 9 * CIN + 1;
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t full[WG_NBUF], empty[WG_NBUF];
@@ -601,7 +646,7 @@ int launch_conv_t(const ConvLaunch& a, cudaStream_t s) {
     const int attr = picgb::opt_in_dynamic_smem((const void*)conv3x3_kernel<CIN, COUT, EPI>, L::BYTES);
     if (attr != PIC_OK) return attr;
     const dim3 grid(a.W / 128, (a.H + a.rows_per_cta - 1) / a.rows_per_cta, a.batch);
-    conv3x3_kernel<CIN, COUT, EPI><<<grid, THREADS, L::BYTES, s>>>(a);
+    conv3x3_kernel<CIN, COUT, EPI><<<grid, CONV_THREADS, L::BYTES, s>>>(a);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PIC_OK : picgb::cuda_fail(e, "conv3x3_kernel launch");
 }
