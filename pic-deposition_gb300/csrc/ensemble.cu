@@ -207,7 +207,14 @@ __global__ void __launch_bounds__(ENS_THREADS, 4) ens_step_kernel(StepArgs a) {
     const size_t nthreads = (size_t)gridDim.x * ENS_THREADS;
     const size_t tid = (size_t)blockIdx.x * ENS_THREADS + threadIdx.x;
 
+    // With both the move and the deposit, the moved quads are deposited straight
+    // from registers (the deposit phase's run sums and segmented warp scan over
+    // the same 128-particle warp layout): the deposit does not read the particles again.
+    const bool fused = a.do_move && a.do_deposit;
     if (a.do_move) {  // gather + push (push.cu move_particles<true, true>), 4 particles per thread
+        const int lane = threadIdx.x & 31;
+        const unsigned upto = (lane == 31) ? FULLM : ((2u << lane) - 1u);
+        const size_t wfirst = tid - (size_t)lane;  // this warp's first thread
         for (int ri = 0; ri < a.nruns; ++ri) {
             const RunDesc& r = a.runs[ri];
             const int N = r.N;
@@ -217,50 +224,91 @@ __global__ void __launch_bounds__(ENS_THREADS, 4) ens_step_kernel(StepArgs a) {
             // field gathers can start with the other fields' loads
             uint4 ncl = make_uint4(0, 0, 0, 0);
             if (tid < nq) ncl = *reinterpret_cast<const uint4*>(a.cell + (q0 + tid) * 4);
-            for (size_t qi = tid; qi < nq; qi += nthreads) {
+            // warp-uniform loop: lanes past the run's end sit out (their quads do not exist)
+            for (size_t qb = wfirst; qb < nq; qb += nthreads) {
+                const size_t qi = qb + (size_t)lane;
+                const bool act = qi < nq;
                 const size_t p0 = (q0 + qi) * 4;
                 uint4 cl = ncl;
                 if (qi + nthreads < nq) ncl = *reinterpret_cast<const uint4*>(a.cell + (q0 + qi + nthreads) * 4);
-                float4 fx = *reinterpret_cast<const float4*>(a.xr + p0);
-                float4 fy = *reinterpret_cast<const float4*>(a.yr + p0);
-                float4 gx = *reinterpret_cast<const float4*>(a.vx + p0);
-                float4 gy = *reinterpret_cast<const float4*>(a.vy + p0);
+                float4 fx = make_float4(0.0f, 0.0f, 0.0f, 0.0f), fy = fx, gx = fx, gy = fx;
                 uint32_t* pc = reinterpret_cast<uint32_t*>(&cl);
                 float *px = reinterpret_cast<float*>(&fx), *py = reinterpret_cast<float*>(&fy);
                 float *pvx = reinterpret_cast<float*>(&gx), *pvy = reinterpret_cast<float*>(&gy);
+                if (act) {
+                    fx = *reinterpret_cast<const float4*>(a.xr + p0);
+                    fy = *reinterpret_cast<const float4*>(a.yr + p0);
+                    gx = *reinterpret_cast<const float4*>(a.vx + p0);
+                    gy = *reinterpret_cast<const float4*>(a.vy + p0);
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const uint32_t local = pc[k] - r.cell_base;
-                    int iy = (int)(local / (uint32_t)N);
-                    int ix = (int)(local - (uint32_t)iy * (uint32_t)N);
-                    float rx = px[k], ry = py[k];
-                    float vxx = pvx[k], vyy = pvy[k];
-                    const int ixp = (ix + 1) % N, iyp = (iy + 1) % N;
-                    const size_t i00 = b0 + (size_t)iy * N + ix, i10 = b0 + (size_t)iy * N + ixp;
-                    const size_t i01 = b0 + (size_t)iyp * N + ix, i11 = b0 + (size_t)iyp * N + ixp;
-                    const float ex = interp_f(a.Exf, i00, i10, i01, i11, rx, ry);
-                    const float ey = interp_f(a.Eyf, i00, i10, i01, i11, rx, ry);
-                    vxx = vxx + (r.coef * ex) * a.dtf;
-                    vyy = vyy + (r.coef * ey) * a.dtf;
-                    drift_f(rx, ix, vxx, a.dtd, N);
-                    drift_f(ry, iy, vyy, a.dtd, N);
-                    pvx[k] = vxx;
-                    pvy[k] = vyy;
-                    px[k] = rx;
-                    py[k] = ry;
-                    pc[k] = r.cell_base + (uint32_t)iy * (uint32_t)N + (uint32_t)ix;
+                    for (int k = 0; k < 4; ++k) {
+                        const uint32_t local = pc[k] - r.cell_base;
+                        int iy = (int)(local / (uint32_t)N);
+                        int ix = (int)(local - (uint32_t)iy * (uint32_t)N);
+                        float rx = px[k], ry = py[k];
+                        float vxx = pvx[k], vyy = pvy[k];
+                        const int ixp = (ix + 1) % N, iyp = (iy + 1) % N;
+                        const size_t i00 = b0 + (size_t)iy * N + ix, i10 = b0 + (size_t)iy * N + ixp;
+                        const size_t i01 = b0 + (size_t)iyp * N + ix, i11 = b0 + (size_t)iyp * N + ixp;
+                        const float ex = interp_f(a.Exf, i00, i10, i01, i11, rx, ry);
+                        const float ey = interp_f(a.Eyf, i00, i10, i01, i11, rx, ry);
+                        vxx = vxx + (r.coef * ex) * a.dtf;
+                        vyy = vyy + (r.coef * ey) * a.dtf;
+                        drift_f(rx, ix, vxx, a.dtd, N);
+                        drift_f(ry, iy, vyy, a.dtd, N);
+                        pvx[k] = vxx;
+                        pvy[k] = vyy;
+                        px[k] = rx;
+                        py[k] = ry;
+                        pc[k] = r.cell_base + (uint32_t)iy * (uint32_t)N + (uint32_t)ix;
+                    }
+                    *reinterpret_cast<uint4*>(a.cell + p0) = cl;
+                    *reinterpret_cast<float4*>(a.xr + p0) = fx;
+                    *reinterpret_cast<float4*>(a.yr + p0) = fy;
+                    *reinterpret_cast<float4*>(a.vx + p0) = gx;
+                    *reinterpret_cast<float4*>(a.vy + p0) = gy;
                 }
-                *reinterpret_cast<uint4*>(a.cell + p0) = cl;
-                *reinterpret_cast<float4*>(a.xr + p0) = fx;
-                *reinterpret_cast<float4*>(a.yr + p0) = fy;
-                *reinterpret_cast<float4*>(a.vx + p0) = gx;
-                *reinterpret_cast<float4*>(a.vy + p0) = gy;
+                if (fused) {  // deposit.cu deposit_runs<CIC> on the moved quads (charge -1)
+                    uint32_t ckey = NO_KEY;
+                    int acc[4] = {0, 0, 0, 0};
+                    if (act) {
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            int val[4];
+                            cic_values(px[k], py[k], -1.0f, val);
+                            if (pc[k] != ckey) {
+                                if (ckey != NO_KEY) flush_cic(a, a.runs, cbase, a.nruns, ckey, acc);
+                                ckey = pc[k];
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) acc[q] = val[q];
+                            } else {
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) acc[q] += val[q];
+                            }
+                        }
+                    }
+                    const uint32_t kprev = __shfl_up_sync(FULLM, ckey, 1);
+                    // segments stop at lane 16: a run total covers <= 64 particles and fits int32
+                    const unsigned H = __ballot_sync(FULLM, lane == 0 || lane == 16 || ckey != kprev);
+                    const int segstart = 31 - __clz(H & upto);
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const bool take = lane - d >= segstart;
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const int o = __shfl_up_sync(FULLM, acc[q], d);
+                            if (take) acc[q] += o;
+                        }
+                    }
+                    const bool tail = (lane == 31) || ((H >> (lane + 1)) & 1u);
+                    if (tail && ckey != NO_KEY) flush_cic(a, a.runs, cbase, a.nruns, ckey, acc);
+                }
             }
         }
-        if (a.do_deposit || a.do_convert)
+        if (fused ? a.do_convert : (a.do_deposit || a.do_convert))
             if (!grid_barrier(a.bar, a.err)) return;
     }
-    if (a.do_deposit) {  // deposit.cu deposit_runs<CIC>, per-run wrap
+    if (a.do_deposit && !fused) {  // deposit.cu deposit_runs<CIC>, per-run wrap
         const int lane = threadIdx.x & 31;
         const size_t gw = (size_t)blockIdx.x * ENS_WARPS + (threadIdx.x >> 5);
         const size_t stride = (size_t)gridDim.x * ENS_WARPS * 128;
