@@ -382,6 +382,10 @@ typedef struct pic_ens_config {
     int sort_interval;  /* cell sort every this many steps (0 = never) */
     int use_graph;
     unsigned seed;
+    double sort_disorder; /* 0: sorts follow sort_interval alone. > 0: also sort when, two steps
+                             earlier, more than this fraction of adjacent particle pairs were out
+                             of cell order after the push (read two steps behind, so the GPU
+                             never waits for the host). Results do not depend on it. */
 } pic_ens_config;
 typedef struct pic_ens_run_info {
     int N, ppc;
@@ -401,6 +405,8 @@ int pic_ens_num_runs(pic_ens* ens, int* n);
 int pic_ens_info(pic_ens* ens, int run, pic_ens_run_info* info);
 int pic_ens_launch_count(pic_ens* ens, long long* n);
 int pic_ens_get_stream(pic_ens* ens, void** stream_out);
+/* Cell sorts the ensemble has done. */
+int pic_ens_sort_count(pic_ens* ens, long long* n);
 /* Run `run`'s particles (positions in cell units, velocities; any pointer may be
  * NULL) in their device order, and its rho and phi (N*N each). */
 int pic_ens_download_run(pic_ens* ens, int run, double* x, double* y, double* vx, double* vy, double* rho,

@@ -82,6 +82,7 @@ struct StepArgs {
     unsigned* bar;   // [0] arrivals, [1] generation
     int* err;
     int do_move, do_deposit, do_convert;
+    unsigned long long* breaks;  // moved particles out of cell order (adjacent pairs), or null
 };
 
 __device__ __forceinline__ uint64_t gtime_ns() {
@@ -211,6 +212,7 @@ __global__ void __launch_bounds__(ENS_THREADS, 4) ens_step_kernel(StepArgs a) {
     // from registers (the deposit phase's run sums and segmented warp scan over
     // the same 128-particle warp layout): the deposit does not read the particles again.
     const bool fused = a.do_move && a.do_deposit;
+    unsigned brk = 0;  // fused: this thread's order breaks
     if (a.do_move) {  // gather + push (push.cu move_particles<true, true>), 4 particles per thread
         const int lane = threadIdx.x & 31;
         const unsigned upto = (lane == 31) ? FULLM : ((2u << lane) - 1u);
@@ -269,6 +271,12 @@ __global__ void __launch_bounds__(ENS_THREADS, 4) ens_step_kernel(StepArgs a) {
                     *reinterpret_cast<float4*>(a.vy + p0) = gy;
                 }
                 if (fused) {  // deposit.cu deposit_runs<CIC> on the moved quads (charge -1)
+                    // disorder: adjacent pairs whose cell key decreases (within the run's range;
+                    // inactive lanes are the warp's last ones, so lane - 1 is active with lane)
+                    const uint32_t prev3 = __shfl_up_sync(FULLM, pc[3], 1);
+                    if (act)
+                        brk += (pc[1] < pc[0]) + (pc[2] < pc[1]) + (pc[3] < pc[2]) +
+                               ((lane > 0 && qi > 0 && pc[0] < prev3) ? 1u : 0u);
                     uint32_t ckey = NO_KEY;
                     int acc[4] = {0, 0, 0, 0};
                     if (act) {
@@ -304,6 +312,11 @@ __global__ void __launch_bounds__(ENS_THREADS, 4) ens_step_kernel(StepArgs a) {
                     if (tail && ckey != NO_KEY) flush_cic(a, a.runs, cbase, a.nruns, ckey, acc);
                 }
             }
+        }
+        if (fused && a.breaks) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) brk += __shfl_xor_sync(FULLM, brk, o);
+            if (lane == 0 && brk) atomicAdd(a.breaks, (unsigned long long)brk);
         }
         if (fused ? a.do_convert : (a.do_deposit || a.do_convert))
             if (!grid_barrier(a.bar, a.err)) return;
@@ -673,6 +686,13 @@ __global__ void ens_energy_final(const RunDesc* __restrict__ runs, const float* 
 
 __global__ void bump_step(int* step) { *step += 1; }
 
+// ring[step] = the order breaks the step's kernel counted; the counter restarts
+__global__ void take_breaks(unsigned long long* counter, unsigned long long* ring, const int* step, int cap) {
+    const int s = *step;
+    if (s < cap) ring[s] = *counter;
+    *counter = 0;
+}
+
 }  // namespace
 
 }  // namespace picgb
@@ -695,6 +715,10 @@ struct pic_ens {
     int hist_cap = 0;
     double dt = 0.1, amp = 0.01, vth = 0.05;
     int sort_interval = 0, use_graph = 1;
+    double sort_disorder = 0.0;   // > 0: also sort on the measured order breaks
+    unsigned long long* breaks = nullptr;       // counter of the step kernel
+    unsigned long long* breaks_ring = nullptr;  // per step of a pic_ens_run call (hist_cap entries)
+    long long sorts = 0;
     long long steps_done = 0;
     int coop_blocks = 0;
     uint32_t en_blocks = 0;  // blocks of the energy sums (all runs)
@@ -746,6 +770,7 @@ StepArgs step_args(pic_ens* e) {
     a.dtd = (float)(e->dt / 1.0);
     a.bar = e->bar;
     a.err = e->err;
+    a.breaks = e->sort_disorder > 0.0 ? e->breaks : nullptr;
     return a;
 }
 
@@ -836,8 +861,16 @@ int energies(pic_ens* e) {
 }
 
 // The step without a sort: persistent kernel, Poisson, energies.
+int take_step_breaks(pic_ens* e) {
+    if (e->sort_disorder <= 0.0) return PIC_OK;
+    take_breaks<<<1, 1, 0, e->c->stream>>>(e->breaks, e->breaks_ring, e->step_ctr, e->hist_cap);
+    e->c->launches++;
+    return check_launch(e->c, "take_breaks");
+}
+
 int plain_step(pic_ens* e) {
     PIC_TRY(launch_step_kernel(e, 1, 1, 1));
+    PIC_TRY(take_step_breaks(e));
     PIC_TRY(poisson(e));
     return energies(e);
 }
@@ -900,9 +933,11 @@ int sorted_step(pic_ens* e) {
     pic_ctx* c = e->c;
     PIC_TRY(launch_step_kernel(e, 1, 0, 0));
     PIC_TRY(sort_particles(c));
+    e->sorts++;
     if (!e->tuned) PIC_TRY(autotune(e));
     PIC_TRY(launch_tiled(e, 0, (int)e->runs.size() - 1));
     PIC_TRY(launch_step_kernel(e, 0, 0, 1));
+    PIC_TRY(take_step_breaks(e));  // zero: the step's deposit ran on sorted particles
     PIC_TRY(poisson(e));
     return energies(e);
 }
@@ -941,6 +976,8 @@ extern "C" {
 int pic_ens_create(const pic_ens_member* runs_in, int nruns, const pic_ens_config* cfg, int device, pic_ens** out) {
     if (!runs_in || nruns <= 0 || nruns > MAX_RUNS || !cfg || !out) return fail(PIC_ERR_ARG, "bad ensemble argument");
     *out = nullptr;
+    if (!(cfg->sort_disorder >= 0.0 && cfg->sort_disorder <= 1.0))
+        return fail(PIC_ERR_ARG, "ensemble sort_disorder must be in [0, 1]");
     std::vector<int> order(nruns);
     for (int i = 0; i < nruns; ++i) {
         const int N = runs_in[i].N, ppc = runs_in[i].ppc;
@@ -961,6 +998,7 @@ int pic_ens_create(const pic_ens_member* runs_in, int nruns, const pic_ens_confi
     e->amp = cfg->amplitude;
     e->vth = cfg->vth;
     e->sort_interval = cfg->sort_interval;
+    e->sort_disorder = cfg->sort_disorder;
     e->use_graph = cfg->use_graph;
     pic_domain d{(double)G, 1.0, (int32_t)G, 1};
     int rc = pic_gpu_create(&d, n, device, &e->c);
@@ -1007,6 +1045,7 @@ int pic_ens_create(const pic_ens_member* runs_in, int nruns, const pic_ens_confi
     e->bar = (unsigned*)A(2 * sizeof(unsigned));
     e->err = (int*)A(sizeof(int));
     e->step_ctr = (int*)A(sizeof(int));
+    e->breaks = (unsigned long long*)A(sizeof(unsigned long long));
     e->en_partial = (double*)A(sizeof(double) * 2 * e->en_blocks);
     if (out_rc == PIC_OK) out_rc = ensure_fields(c);
     if (out_rc == PIC_OK) out_rc = upload_runs(e);
@@ -1093,7 +1132,7 @@ int pic_ens_destroy(pic_ens* e) {
         cufftDestroy(b.inv);
     }
     void* ptrs[] = {e->druns, e->dmass, e->bar, e->err, e->step_ctr, e->fe_hist, e->ke_hist, e->en_partial,
-                    e->rhs_all, e->spec_all};
+                    e->rhs_all, e->spec_all, e->breaks, e->breaks_ring};
     for (void* p : ptrs) dfree(p);
     if (e->c) pic_gpu_destroy(e->c);
     delete e;
@@ -1108,9 +1147,11 @@ int pic_ens_run(pic_ens* e, int steps, double* field_energy, double* kinetic_ene
     if (steps > e->hist_cap) {
         dfree(e->fe_hist);
         dfree(e->ke_hist);
+        dfree(e->breaks_ring);
         int rc = PIC_OK;
         e->fe_hist = (double*)dalloc((size_t)steps * nr * 8, &rc);
         if (!rc) e->ke_hist = (double*)dalloc((size_t)steps * nr * 8, &rc);
+        if (!rc) e->breaks_ring = (unsigned long long*)dalloc((size_t)steps * 8, &rc);
         if (rc) {
             e->hist_cap = 0;
             return rc;
@@ -1119,18 +1160,59 @@ int pic_ens_run(pic_ens* e, int steps, double* field_energy, double* kinetic_ene
         for (auto& g : e->graphs) cudaGraphExecDestroy(g.exec);
         e->graphs.clear();
     }
-    PIC_CUDA_TRY(cudaMemsetAsync(e->step_ctr, 0, sizeof(int), c->stream));
-    for (int s = 0; s < steps; ++s) {
-        const bool sort = e->sort_interval > 0 && (e->steps_done % e->sort_interval) == 0;
-        if (sort) {
-            PIC_TRY(sorted_step(e));
-        } else if (e->use_graph) {
-            PIC_TRY(graph_step(e));
-        } else {
-            PIC_TRY(plain_step(e));
+    // sorts on measured disorder: the breaks of step s - 2 decide step s (copied to
+    // page-locked memory after each step; the host waits for a step two behind)
+    const bool by_disorder = e->sort_disorder > 0.0;
+    unsigned long long* brk_h = nullptr;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    auto release = [&]() {
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        if (brk_h) cudaFreeHost(brk_h);
+    };
+    if (by_disorder && steps > 0) {
+        if (cudaHostAlloc((void**)&brk_h, (size_t)steps * 8, 0) != cudaSuccess) {
+            brk_h = nullptr;
+            return fail(PIC_ERR_NOMEM, "pinned allocation");
         }
-        e->steps_done++;
+        for (int i = 0; i < 3; ++i)
+            if (cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess) {
+                release();
+                return fail(PIC_ERR_CUDA, "cudaEventCreate");
+            }
     }
+    const int loop_rc = [&]() -> int {
+        PIC_CUDA_TRY(cudaMemsetAsync(e->step_ctr, 0, sizeof(int), c->stream));
+        if (by_disorder) PIC_CUDA_TRY(cudaMemsetAsync(e->breaks, 0, sizeof(unsigned long long), c->stream));
+        const double limit = e->sort_disorder * (double)c->n;
+        int last_sort = -1;
+        for (int s = 0; s < steps; ++s) {
+            bool sort = e->sort_interval > 0 && (e->steps_done % e->sort_interval) == 0;
+            const int m = s - 2;
+            if (by_disorder && !sort && m >= 0 && m > last_sort) {
+                PIC_CUDA_TRY(cudaEventSynchronize(ev[m % 3]));
+                sort = (double)brk_h[m] > limit;
+            }
+            if (sort) {
+                last_sort = s;
+                PIC_TRY(sorted_step(e));
+            } else if (e->use_graph) {
+                PIC_TRY(graph_step(e));
+            } else {
+                PIC_TRY(plain_step(e));
+            }
+            if (by_disorder) {
+                PIC_CUDA_TRY(cudaMemcpyAsync(brk_h + s, e->breaks_ring + s, 8, cudaMemcpyDeviceToHost, c->stream));
+                PIC_CUDA_TRY(cudaEventRecord(ev[s % 3], c->stream));
+            }
+            e->steps_done++;
+        }
+        return PIC_OK;
+    }();
+    const cudaError_t se = cudaStreamSynchronize(c->stream);
+    release();
+    PIC_TRY(loop_rc);
+    if (se != cudaSuccess) return cuda_fail(se, "cudaStreamSynchronize");
     int herr = 0;
     PIC_CUDA_TRY(cudaMemcpyAsync(&herr, e->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     if (field_energy)
@@ -1141,6 +1223,12 @@ int pic_ens_run(pic_ens* e, int steps, double* field_energy, double* kinetic_ene
                                      c->stream));
     PIC_TRY(pic_gpu_synchronize(c));
     if (herr) return fail(PIC_ERR_TIMEOUT, "ensemble: a grid-wide barrier timed out");
+    return PIC_OK;
+}
+
+int pic_ens_sort_count(pic_ens* e, long long* n) {
+    if (!e || !n) return fail(PIC_ERR_ARG, "bad argument");
+    *n = e->sorts;
     return PIC_OK;
 }
 

@@ -237,7 +237,7 @@ class EnsMember(C.Structure):
 
 class EnsConfig(C.Structure):
     _fields_ = [("dt", C.c_double), ("amplitude", C.c_double), ("vth", C.c_double), ("sort_interval", C.c_int),
-                ("use_graph", C.c_int), ("seed", C.c_uint)]
+                ("use_graph", C.c_int), ("seed", C.c_uint), ("sort_disorder", C.c_double)]
 
 
 class EnsRunInfo(C.Structure):
@@ -252,6 +252,7 @@ _SIGS += [
     ("pic_ens_num_runs", [_vp, C.POINTER(C.c_int)]),
     ("pic_ens_info", [_vp, C.c_int, C.POINTER(EnsRunInfo)]),
     ("pic_ens_launch_count", [_vp, C.POINTER(C.c_longlong)]),
+    ("pic_ens_sort_count", [_vp, C.POINTER(C.c_longlong)]),
     ("pic_ens_get_stream", [_vp, C.POINTER(_vp)]),
     ("pic_ens_download_run", [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
 ]
@@ -262,9 +263,10 @@ class Ensemble:
     Runs are reordered by grid size; info(r) gives run r's setup in that order."""
 
     def __init__(self, runs, dt=0.1, amplitude=0.01, vth=0.05, sort_interval=20, use_graph=True, seed=1,
-                 device=0):
+                 device=0, sort_disorder=0.0):
         arr = (EnsMember * len(runs))(*[EnsMember(int(n), int(p), int(s)) for n, p, s in runs])
-        cfg = EnsConfig(float(dt), float(amplitude), float(vth), int(sort_interval), int(use_graph), int(seed))
+        cfg = EnsConfig(float(dt), float(amplitude), float(vth), int(sort_interval), int(use_graph), int(seed),
+                        float(sort_disorder))
         h = _vp()
         _check(lib().pic_ens_create(arr, len(runs), C.byref(cfg), int(device), C.byref(h)))
         self.h = h
@@ -310,6 +312,12 @@ class Ensemble:
     def launch_count(self):
         n = C.c_longlong()
         _check(lib().pic_ens_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def sort_count(self):
+        """Cell sorts the ensemble has done (pic_ens_sort_count)."""
+        n = C.c_longlong()
+        _check(lib().pic_ens_sort_count(self.h, C.byref(n)))
         return n.value
 
     def stream(self):

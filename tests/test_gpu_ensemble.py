@@ -81,3 +81,27 @@ def test_mode_growth_rate(pg):
     for r in range(fe.shape[1]):
         slope = (np.log(fe[39, r]) - np.log(fe[14, r])) / (25 * DT)
         assert 1.7 < slope < 2.2, (r, slope)
+
+
+def test_sort_on_disorder_changes_nothing(pg):
+    """pic_ens_config.sort_disorder: sorts triggered by the order breaks the step
+    kernel counts (the generated stream starts out of cell order) happen, and the
+    field energies, grids and particle sets equal those of an ensemble that never
+    sorts, bit for bit."""
+    res = []
+    for kw in (dict(sort_interval=0), dict(sort_interval=0, sort_disorder=1e-6)):
+        with pg.Ensemble(RUNS, dt=DT, use_graph=True, **kw) as e:
+            fe, ke = e.run(9)
+            states = [e.download_run(r) for r in range(len(RUNS))]
+            sorts = e.sort_count()
+        res.append((fe, ke, states, sorts))
+    (fe0, ke0, s0, n0), (fe1, ke1, s1, n1) = res
+    assert n0 == 0 and n1 >= 1
+    assert np.array_equal(fe0, fe1)
+    for a, b in zip(s0, s1):
+        assert np.array_equal(a["rho"], b["rho"]) and np.array_equal(a["phi"], b["phi"])
+        ka = np.lexsort((a["vy"], a["vx"], a["y"], a["x"]))
+        kb = np.lexsort((b["vy"], b["vx"], b["y"], b["x"]))
+        for k in ("x", "y", "vx", "vy"):
+            assert np.array_equal(a[k][ka], b[k][kb])
+    assert np.allclose(ke0, ke1, rtol=1e-6)
