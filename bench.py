@@ -484,8 +484,10 @@ def run_gpu(args, d: Dist):
     ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
     ctx.profile(True)
     _, perm, _ = ctx.sort(perm=True)
-    ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
-    ctx.sort()
+    ctx.profile_read("sort")  # the first sort also allocates its scratch arrays: not timed
+    for _ in range(2):
+        ctx.upload(p["x"], p["y"], p["q"], p["vx"], p["vy"], p["m"])
+        ctx.sort()
     sort_ms, sort_cnt = ctx.profile_read("sort")
     sort_ms /= max(sort_cnt, 1)
     # unsorted (random order) deposits for reference numbers: use the random-order upload

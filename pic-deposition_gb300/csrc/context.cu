@@ -252,6 +252,7 @@ __global__ void convert_particles(ConvertArgs a) {
         a.fvy[o] = fvy;
         a.fq[o] = fq;
         if (a.fm) a.fm[o] = a.m ? __double2float_rn(a.m[i]) : 1.0f;
+        if (o == 0) a.st->q_raw0 = fq;
         aq = fabsf(fq);
         avx = fabsf(fvx);
         avy = fabsf(fvy);
@@ -286,32 +287,52 @@ static int ensure_copy_stream(pic_ctx* c) {
     return PIC_OK;
 }
 
-// q <- q / max|q| (FP32 IEEE division): a uniform |q| becomes exactly +-1.
-__global__ void normalize_charge(float* __restrict__ q, size_t n, const DevStats* st) {
-    const float mq = load_maxq(st);
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) q[i] = mq > 0.0f ? __fdiv_rn(q[i], mq) : 0.0f;
-}
-
-// Flags stored charges that differ from the first particle's (bitwise).
-__global__ void check_uniform_charge(const float* __restrict__ q, size_t n, DevStats* st) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const float q0 = q[0];
-    if (i == 0) st->q_first = q0;
-    const bool diff = i < n && __float_as_uint(q[i]) != __float_as_uint(q0);
-    if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(&st->q_mixed, 1u);
-}
-
-// Counts adjacent pairs out of cell order (0 => the upload is already sorted):
-// per warp by ballot, per block in shared memory, one global atomic per block.
-__global__ void count_order_breaks(const uint32_t* __restrict__ cell, size_t n, DevStats* st) {
+// One pass over the stored charges and keys after the conversion, four
+// particles per thread (16-byte loads and stores; the arrays are padded past the
+// last particle and 16-byte aligned):
+//  * q <- q / max|q| (FP32 IEEE division): a uniform |q| becomes exactly +-1;
+//  * a flag when a normalised charge differs (bitwise) from the first
+//    particle's (normalised from its charge as converted, which every thread
+//    reads before any store);
+//  * the count of adjacent pairs out of cell order (0: the upload is already
+//    sorted): per thread, the key before its four from the previous lane (lane
+//    0 loads it), summed per block, one global atomic per block.
+__global__ void finish_upload(float* __restrict__ q, const uint32_t* __restrict__ cell, size_t n, DevStats* st) {
     __shared__ unsigned s_breaks;
     if (threadIdx.x == 0) s_breaks = 0;
     __syncthreads();
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const bool brk = i < n && cell[i] < cell[i - 1];
-    const unsigned b = __ballot_sync(0xffffffffu, brk);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&s_breaks, (unsigned)__popc(b));
+    const float mq = load_maxq(st);
+    const float q0 = mq > 0.0f ? __fdiv_rn(st->q_raw0, mq) : 0.0f;
+    const size_t i0 = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    const bool act = i0 < n;
+    uint4 kv = make_uint4(0u, 0u, 0u, 0u);
+    float4 qv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (act) {
+        kv = *reinterpret_cast<const uint4*>(cell + i0);
+        qv = *reinterpret_cast<const float4*>(q + i0);
+    }
+    uint32_t before = __shfl_up_sync(0xffffffffu, kv.w, 1);
+    bool diff = false;
+    unsigned brk = 0;
+    if (act) {
+        if ((threadIdx.x & 31) == 0 && i0 > 0) before = cell[i0 - 1];
+        const int cnt = (n - i0) < 4 ? (int)(n - i0) : 4;
+        float w[4] = {qv.x, qv.y, qv.z, qv.w};
+        const uint32_t k[4] = {kv.x, kv.y, kv.z, kv.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j < cnt) {
+                w[j] = mq > 0.0f ? __fdiv_rn(w[j], mq) : 0.0f;
+                diff |= __float_as_uint(w[j]) != __float_as_uint(q0);
+                brk += (j == 0 ? (i0 > 0 && k[0] < before) : (k[j] < k[j - 1])) ? 1u : 0u;
+            }
+        }
+        *reinterpret_cast<float4*>(q + i0) = make_float4(w[0], w[1], w[2], w[3]);
+        if (i0 == 0) st->q_first = q0;
+    }
+    if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(&st->q_mixed, 1u);
+    brk = __reduce_add_sync(0xffffffffu, brk);
+    if ((threadIdx.x & 31) == 0 && brk) atomicAdd(&s_breaks, brk);
     __syncthreads();
     if (threadIdx.x == 0 && s_breaks) atomicAdd(&st->order_breaks, s_breaks);
 }
@@ -552,14 +573,8 @@ int pic_gpu_upload_particles(pic_ctx* c, const double* x, const double* y, const
     c->qsum_valid = 0;
     c->qn_uniform = 0.0f;
     if (n > 0) {
-        normalize_charge<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->q, n, c->dstats);
-        PIC_TRY(check_launch(c, "normalize_charge"));
-        check_uniform_charge<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->q, n, c->dstats);
-        PIC_TRY(check_launch(c, "check_uniform_charge"));
-    }
-    if (n > 1) {
-        count_order_breaks<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->cell, n, c->dstats);
-        PIC_TRY(check_launch(c, "count_order_breaks"));
+        finish_upload<<<(unsigned)((n + 1023) / 1024), 256, 0, c->stream>>>(c->q, c->cell, n, c->dstats);
+        PIC_TRY(check_launch(c, "finish_upload"));
     }
     PIC_TRY(pic_gpu_synchronize(c));
     DevStats st;

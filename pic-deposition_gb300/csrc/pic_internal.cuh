@@ -24,6 +24,7 @@ struct DevStats {
     unsigned int order_breaks;  // uploads: count of i with cell[i] < cell[i-1]
     unsigned int q_mixed;       // uploads: nonzero when the stored charges differ
     float q_first;              // uploads: the first particle's stored charge
+    float q_raw0;               // uploads: the first particle's charge before normalisation
     unsigned long long moved;   // deposits between sorts: particles found outside their sorted cell
 };
 

@@ -29,28 +29,45 @@ constexpr int RS_WARP_ITEMS = RS_TILE / RS_WARPS;   // 512 keys per warp
 constexpr int RS_MAX_BITS = 10;                     // widest digit (wider ones spill, one CTA per SM)
 constexpr int RS_MAX_PAYLOAD = 7;                   // xr yr vx vy q m perm
 
-// Digit histogram of one tile. When all 32 keys of a warp instruction share a
-// digit (cell-ordered input) they are counted with one shared atomic.
+// Digit histogram of one tile. Each thread counts 16 consecutive keys (four
+// 16-byte loads, all issued before the first count) and adds each run of equal
+// digits with one shared atomic: about one atomic per thread for cell-ordered
+// input. Keys are read with the streaming (evict-first) policy.
 template <int BITS>
 __global__ void __launch_bounds__(RS_THREADS) radix_histogram(const uint32_t* __restrict__ keys, size_t n,
                                                               int shift, uint32_t mask, uint32_t* __restrict__ counts,
                                                               unsigned num_tiles) {
     constexpr int RADIX = 1 << BITS;
+    static_assert(RS_ITEMS % 4 == 0, "whole 16-byte loads");
     __shared__ uint32_t hist[RADIX];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < RADIX; i += RS_THREADS) hist[i] = 0;
+    // key arrays hold PARTICLE_PAD words past the last particle and start 16-byte
+    // aligned, so a thread's four loads stay inside the allocation
+    const size_t base = (size_t)blockIdx.x * RS_TILE + (size_t)threadIdx.x * RS_ITEMS;
+    uint4 v[RS_ITEMS / 4];
+    if (base < n) {
+#pragma unroll
+        for (int j = 0; j < RS_ITEMS / 4; ++j) v[j] = __ldcs(reinterpret_cast<const uint4*>(keys + base) + j);
+    }
     __syncthreads();
-    const size_t base = (size_t)blockIdx.x * RS_TILE + (size_t)warp * RS_WARP_ITEMS;
-#pragma unroll 4
-    for (int r = 0; r < RS_WARP_ITEMS / 32; ++r) {
-        const size_t i = base + (size_t)r * 32 + lane;
-        const uint32_t d = i < n ? (keys[i] >> shift) & mask : 0xffffffffu;
-        const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
-        if (__all_sync(0xffffffffu, d == d0)) {
-            if (lane == 0 && d0 != 0xffffffffu) atomicAdd(&hist[d0], 32u);
-        } else if (d != 0xffffffffu) {
-            atomicAdd(&hist[d], 1u);
+    if (base < n) {
+        const int cnt = (n - base) < (size_t)RS_ITEMS ? (int)(n - base) : RS_ITEMS;
+        uint32_t run_d = (v[0].x >> shift) & mask, run_n = 0;
+#pragma unroll
+        for (int j = 0; j < RS_ITEMS; ++j) {
+            if (j < cnt) {
+                const uint4& w = v[j >> 2];
+                const uint32_t kj = (j & 3) == 0 ? w.x : (j & 3) == 1 ? w.y : (j & 3) == 2 ? w.z : w.w;
+                const uint32_t d = (kj >> shift) & mask;
+                if (d != run_d) {
+                    atomicAdd(&hist[run_d], run_n);
+                    run_d = d;
+                    run_n = 0;
+                }
+                ++run_n;
+            }
         }
+        atomicAdd(&hist[run_d], run_n);
     }
     __syncthreads();
     for (int d = threadIdx.x; d < RADIX; d += RS_THREADS) counts[(size_t)d * num_tiles + blockIdx.x] = hist[d];
@@ -98,7 +115,7 @@ __global__ void __launch_bounds__(RS_THREADS, 2) radix_scatter(const uint32_t* _
     for (int r = 0; r < RS_ITEMS; ++r) {
         const size_t i = base + (size_t)r * 32 + lane;
         const bool ok = i < n;
-        k[r] = ok ? keys_in[i] : 0u;
+        k[r] = ok ? __ldcs(keys_in + i) : 0u;
         // lanes with the same digit form one group; its lowest lane advances the
         // warp's counter for that digit by the group size and broadcasts the old value
         const uint32_t d = ok ? ((k[r] >> shift) & mask) : 0xffffffffu;
@@ -165,7 +182,7 @@ __global__ void __launch_bounds__(RS_THREADS, 2) radix_scatter(const uint32_t* _
 #pragma unroll
         for (int r = 0; r < RS_ITEMS; ++r) {
             const size_t i = base + (size_t)r * 32 + lane;
-            pv[r] = rank[r] == 0xffffffffu ? 0u : (src ? src[i] : (uint32_t)i);
+            pv[r] = rank[r] == 0xffffffffu ? 0u : (src ? __ldcs(src + i) : (uint32_t)i);
         }
     };
     if (pay.count > 0) load_field(0);
@@ -197,42 +214,61 @@ __global__ void iota_u32(uint32_t* __restrict__ out, size_t n) {
     if (i < n) out[i] = (uint32_t)i;
 }
 
-// offsets[c] = the first index whose key is >= c, from cell-ordered keys: thread
-// i writes i into offsets[keys[i-1]+1 .. keys[i]] (thread 0 from cell 0), the
-// last thread also offsets[keys[n-1]+1 .. G]. Every entry is written once.
+// offsets[c] = the first index whose key is >= c, from cell-ordered keys: index
+// i writes i into offsets[keys[i-1]+1 .. keys[i]] (index 0 from cell 0), the
+// last index also offsets[keys[n-1]+1 .. G]. Every entry is written once. Four
+// keys per thread (one 16-byte load; the key before them comes from the
+// previous lane, lane 0 loads it). A range of more than OFS_SHORT cells (empty
+// cells between two particles) is filled by the whole warp, 32 entries per store
+// instruction, so a sparse or lopsided distribution costs no long serial loop.
+constexpr uint32_t OFS_SHORT = 16;
+
 __global__ void offsets_from_sorted(const uint32_t* __restrict__ keys, size_t n, uint32_t G,
                                     uint32_t* __restrict__ offsets, DevStats* st) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t k = keys[i];
-    if (k >= G) {
-        set_dev_error(st, DEV_BAD_CELL, (unsigned int)i);
-        k = G;
-    }
-    uint32_t prev = 0;
-    if (i > 0) {
-        prev = keys[i - 1];
-        prev = prev >= G ? G : prev + 1;
-    }
-    for (uint32_t c = prev; c <= k && c < G; ++c) offsets[c] = (uint32_t)i;
-    if (i + 1 == n)
-        for (uint32_t c = k + 1; c <= G; ++c) offsets[c] = (uint32_t)n;
-}
-
-// Per-cell counts of the sorted keys; runs of equal keys inside a warp are
-// aggregated (sorted input => one atomic per run).
-__global__ void cell_histogram(const uint32_t* __restrict__ keys, size_t n, uint32_t G, uint32_t* __restrict__ cnt,
-                               DevStats* st) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool ok = i < n;
-    uint32_t k = ok ? keys[i] : 0xffffffffu;
-    if (ok && k >= G) {
-        set_dev_error(st, DEV_BAD_CELL, (unsigned int)i);
-        k = 0xfffffffeu;
-    }
-    const unsigned peers = __match_any_sync(0xffffffffu, k);
     const int lane = threadIdx.x & 31;
-    if (ok && k < G && lane == __ffs(peers) - 1) atomicAdd(&cnt[k], (uint32_t)__popc(peers));
+    const size_t i0 = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    const bool act = i0 < n;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (act) v = __ldcs(reinterpret_cast<const uint4*>(keys + i0));  // padded, 16-byte aligned array
+    uint32_t before = __shfl_up_sync(0xffffffffu, v.w, 1);
+    if (act && lane == 0 && i0 > 0) before = keys[i0 - 1];
+    // cells [from, end) get val; every lane of the warp takes part
+    auto fill = [&](uint32_t from, uint32_t end, uint32_t val, bool valid) {
+        const bool lng = valid && end > from + OFS_SHORT;
+        if (valid && !lng)
+            for (uint32_t c = from; c < end; ++c) offsets[c] = val;
+        unsigned m = __ballot_sync(0xffffffffu, lng);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1u;
+            const uint32_t f = __shfl_sync(0xffffffffu, from, src), e = __shfl_sync(0xffffffffu, end, src);
+            const uint32_t x = __shfl_sync(0xffffffffu, val, src);
+            for (uint32_t c = f + (uint32_t)lane; c < e; c += 32u) offsets[c] = x;
+        }
+    };
+    const uint32_t k[4] = {v.x, v.y, v.z, v.w};
+    const int cnt = act ? ((n - i0) < 4 ? (int)(n - i0) : 4) : 0;
+    uint32_t from = (act && i0 > 0) ? (before >= G ? G : before + 1u) : 0u;
+    bool tail = false;
+    uint32_t tail_from = G + 1u;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const bool ok = j < cnt;
+        uint32_t kj = ok ? k[j] : 0u;
+        if (ok && kj >= G) {
+            set_dev_error(st, DEV_BAD_CELL, (unsigned int)(i0 + j));
+            kj = G;
+        }
+        fill(from, kj < G ? kj + 1u : G, (uint32_t)(i0 + j), ok);
+        if (ok) {
+            from = kj >= G ? G : kj + 1u;
+            if (i0 + j + 1 == n && kj < G) {
+                tail = true;
+                tail_from = kj + 1u;
+            }
+        }
+    }
+    fill(tail_from, G + 1u, (uint32_t)n, tail);
 }
 
 int ensure_sort_scratch(pic_ctx* c) {
@@ -267,15 +303,16 @@ int ensure_sort_scratch(pic_ctx* c) {
     return PIC_OK;
 }
 
-// Offsets of the (sorted) keys: histogram + exclusive scan over G+1 entries.
+// Offsets of cell-ordered keys (every caller's keys are: a sort's output, an
+// upload found in order, a one-cell grid).
 int build_offsets(pic_ctx* c, const uint32_t* keys) {
-    PIC_CUDA_TRY(cudaMemsetAsync(c->offsets, 0, (c->G + 1) * 4, c->stream));
-    if (c->n) {
-        cell_histogram<<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(keys, c->n, (uint32_t)c->G, c->offsets,
-                                                                              c->dstats);
-        PIC_TRY(check_launch(c, "cell_histogram"));
+    if (c->n == 0) {
+        PIC_CUDA_TRY(cudaMemsetAsync(c->offsets, 0, (c->G + 1) * 4, c->stream));
+        return PIC_OK;
     }
-    return exclusive_scan_u32(c, c->offsets, c->G + 1);
+    offsets_from_sorted<<<(unsigned)((c->n + 1023) / 1024), 256, 0, c->stream>>>(keys, c->n, (uint32_t)c->G,
+                                                                                  c->offsets, c->dstats);
+    return check_launch(c, "offsets_from_sorted");
 }
 
 template <int BITS>
@@ -345,9 +382,7 @@ int sort_particles(pic_ctx* c, bool perm) {
         if (perm) std::swap(c->idx_a, c->idx_b);
         for (int j = 0; j < nf; ++j) std::swap(*slots[fields[j]], c->alt[fields[j]]);
     }
-    offsets_from_sorted<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->cell, n, (uint32_t)c->G, c->offsets,
-                                                                             c->dstats);
-    PIC_TRY(check_launch(c, "offsets_from_sorted"));
+    PIC_TRY(build_offsets(c, c->cell));
     c->sorted = 1;
     c->part_valid = 1;
     return PIC_OK;

@@ -89,3 +89,34 @@ def test_sort_twice_is_identity(pg):
 def test_sort_config2_full_size(port, pg):
     p = workloads.density_cos(1024, 1024, 64, 0.01, 0.1, seed=42)
     check_sort(port, pg, 1024, 1024, 1024.0, 1024.0, p)
+
+
+def test_in_order_upload_sparse_offsets(port, pg):
+    """An upload already in cell order gets its offsets without a sort; long runs
+    of empty cells are filled by whole warps. Particles in three clusters of a
+    512 x 512 grid (the first cell, mid-grid, the last cell) deposit as the
+    oracle does, and a later sort keeps the order (identity permutation) and
+    gives the offsets of a stable counting sort."""
+    nx = ny = 512
+    rng = np.random.default_rng(8)
+    xs, ys = [], []
+    for cx, cy in ((0.2, 0.3), (200.5, 311.5), (511.6, 511.4)):
+        xs.append(np.clip(cx + rng.normal(0.0, 0.8, 3000), 0.0, 511.999))
+        ys.append(np.clip(cy + rng.normal(0.0, 0.8, 3000), 0.0, 511.999))
+    x, y = np.concatenate(xs), np.concatenate(ys)
+    order = np.argsort(np.floor(y).astype(np.int64) * nx + np.floor(x).astype(np.int64), kind="stable")
+    p = {"x": x[order], "y": y[order], "q": np.full(len(x), -1.0)}
+    with pg.Context(nx, ny, 512.0, 512.0, len(x)) as c:
+        c.upload(p["x"], p["y"], p["q"])
+        assert c.is_sorted()
+        c.deposit(1, 0.0)
+        acc, unit = c.rho_fixed()
+        lay = c.device_layout()
+        _, perm, offs = c.sort(keys=True, perm=True, offsets=True)
+    _, maxq = port.normalize_charge(p["q"])
+    want, wunit = port.deposit_fixed(nx, ny, 512.0, 512.0, 1, lay["cell"], lay["xr"], lay["yr"], lay["q"], maxq,
+                                     lay["vx"], lay["vy"], 0.0)
+    assert unit == wunit and np.array_equal(acc, want)
+    assert np.array_equal(perm, np.arange(len(x), dtype=np.uint32))
+    _, _, wo = port.stable_sort_keys(lay["cell"], nx * ny)
+    assert np.array_equal(offs, wo)
