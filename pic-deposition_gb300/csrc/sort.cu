@@ -219,9 +219,28 @@ __global__ void iota_u32(uint32_t* __restrict__ out, size_t n) {
 // last index also offsets[keys[n-1]+1 .. G]. Every entry is written once. Four
 // keys per thread (one 16-byte load; the key before them comes from the
 // previous lane, lane 0 loads it). A range of more than OFS_SHORT cells (empty
-// cells between two particles) is filled by the whole warp, 32 entries per store
+// cells between two particles) is left to the whole warp, 32 entries per store
 // instruction, so a sparse or lopsided distribution costs no long serial loop.
 constexpr uint32_t OFS_SHORT = 16;
+
+// Range j of a thread's four keys k (j = 4: the cells after the last particle):
+// cells [from, end) get val; false when there is none.
+__device__ __forceinline__ bool offsets_range(int j, const uint32_t (&k)[4], uint32_t before, size_t i0, int cnt,
+                                              size_t n, uint32_t G, uint32_t& from, uint32_t& end, uint32_t& val) {
+    if (j < 4) {
+        if (j >= cnt) return false;
+        const uint32_t prev = j == 0 ? before : k[j - 1];
+        from = (j == 0 && i0 == 0) ? 0u : (prev >= G ? G : prev + 1u);
+        end = k[j] < G ? k[j] + 1u : G;
+        val = (uint32_t)(i0 + j);
+        return true;
+    }
+    if (cnt == 0 || i0 + (size_t)cnt != n || k[cnt - 1] >= G) return false;
+    from = k[cnt - 1] + 1u;
+    end = G + 1u;
+    val = (uint32_t)n;
+    return true;
+}
 
 __global__ void offsets_from_sorted(const uint32_t* __restrict__ keys, size_t n, uint32_t G,
                                     uint32_t* __restrict__ offsets, DevStats* st) {
@@ -232,43 +251,38 @@ __global__ void offsets_from_sorted(const uint32_t* __restrict__ keys, size_t n,
     if (act) v = __ldcs(reinterpret_cast<const uint4*>(keys + i0));  // padded, 16-byte aligned array
     uint32_t before = __shfl_up_sync(0xffffffffu, v.w, 1);
     if (act && lane == 0 && i0 > 0) before = keys[i0 - 1];
-    // cells [from, end) get val; every lane of the warp takes part
-    auto fill = [&](uint32_t from, uint32_t end, uint32_t val, bool valid) {
-        const bool lng = valid && end > from + OFS_SHORT;
-        if (valid && !lng)
-            for (uint32_t c = from; c < end; ++c) offsets[c] = val;
-        unsigned m = __ballot_sync(0xffffffffu, lng);
-        while (m) {
-            const int src = __ffs(m) - 1;
-            m &= m - 1u;
-            const uint32_t f = __shfl_sync(0xffffffffu, from, src), e = __shfl_sync(0xffffffffu, end, src);
-            const uint32_t x = __shfl_sync(0xffffffffu, val, src);
-            for (uint32_t c = f + (uint32_t)lane; c < e; c += 32u) offsets[c] = x;
-        }
-    };
     const uint32_t k[4] = {v.x, v.y, v.z, v.w};
     const int cnt = act ? ((n - i0) < 4 ? (int)(n - i0) : 4) : 0;
-    uint32_t from = (act && i0 > 0) ? (before >= G ? G : before + 1u) : 0u;
-    bool tail = false;
-    uint32_t tail_from = G + 1u;
+    for (int j = 0; j < cnt; ++j)
+        if (k[j] >= G) set_dev_error(st, DEV_BAD_CELL, (unsigned int)(i0 + j));
+    unsigned longs = 0;  // ranges left to the warp
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const bool ok = j < cnt;
-        uint32_t kj = ok ? k[j] : 0u;
-        if (ok && kj >= G) {
-            set_dev_error(st, DEV_BAD_CELL, (unsigned int)(i0 + j));
-            kj = G;
-        }
-        fill(from, kj < G ? kj + 1u : G, (uint32_t)(i0 + j), ok);
-        if (ok) {
-            from = kj >= G ? G : kj + 1u;
-            if (i0 + j + 1 == n && kj < G) {
-                tail = true;
-                tail_from = kj + 1u;
-            }
+    for (int j = 0; j < 5; ++j) {
+        uint32_t from, end, val;
+        if (offsets_range(j, k, before, i0, cnt, n, G, from, end, val)) {
+            if (end > from + OFS_SHORT)
+                longs |= 1u << j;
+            else
+                for (uint32_t c = from; c < end; ++c) offsets[c] = val;
         }
     }
-    fill(tail_from, G + 1u, (uint32_t)n, tail);
+    unsigned m = __ballot_sync(0xffffffffu, longs != 0);
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1u;
+        const unsigned sl = __shfl_sync(0xffffffffu, longs, src);
+        const uint32_t sk[4] = {__shfl_sync(0xffffffffu, k[0], src), __shfl_sync(0xffffffffu, k[1], src),
+                                __shfl_sync(0xffffffffu, k[2], src), __shfl_sync(0xffffffffu, k[3], src)};
+        const uint32_t sb = __shfl_sync(0xffffffffu, before, src);
+        const int sc = __shfl_sync(0xffffffffu, cnt, src);
+        const size_t si = i0 + 4 * (size_t)(src - lane);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            uint32_t from, end, val;
+            if (((sl >> j) & 1u) && offsets_range(j, sk, sb, si, sc, n, G, from, end, val))
+                for (uint32_t c = from + (uint32_t)lane; c < end; c += 32u) offsets[c] = val;
+        }
+    }
 }
 
 int ensure_sort_scratch(pic_ctx* c) {
