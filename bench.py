@@ -821,7 +821,10 @@ def run_config3(args):
     out.update({"ms_per_step": ms / steps, "particle_steps_per_s": n * steps / (ms * 1e-3),
                 "energy_drift_at_steps": {str(k): float(drift[k]) for k in marks},
                 "max_abs_energy_drift": float(np.max(np.abs(drift))),
-                "max_charge_error": float(np.max(h[:, 0]))})
+                "max_charge_error": float(np.max(h[:, 0])),
+                "charge_error_note": "pic::computeDiagnostics' charge_error, |integral of rho - particle charge| / "
+                                     "sum |q|: rho includes the neutralising background (+1 in total) and the "
+                                     "particles carry -1, so a neutral plasma reads 1 by construction"})
     return out
 
 

@@ -91,7 +91,14 @@ struct DepArgs {
     int tile_w, tile_h, tiles_x;
     float qc;  // nonzero: every particle's stored charge (the charge stream is not read)
     DevStats* st;
+    // non-null: the kernel deposits only when *gate == gate_when (the choice
+    // between the cell kernel and the any-order kernel between sorts is made on
+    // the device, so a captured step keeps one shape)
+    const unsigned int* gate;
+    unsigned int gate_when;
 };
+
+__device__ __forceinline__ bool gated_off(const DepArgs& a) { return a.gate && *a.gate != a.gate_when; }
 
 // ---- one axis of a frame. Returns false when an Esirkepov move needs the general loop.
 template <int S>
@@ -396,6 +403,7 @@ __device__ __forceinline__ void flush_global_nd(const DepArgs& a, uint32_t key, 
 // sorts of a time-stepping loop.
 template <int S>
 __global__ void __launch_bounds__(DEP_THREADS) deposit_runs(DepArgs a) {
+    if (gated_off(a)) return;
     constexpr int NX = Frame<S>::NX, V = Frame<S>::V;
     constexpr int NV = NX * NX;
     const int lane = threadIdx.x & 31;
@@ -819,6 +827,7 @@ __device__ __forceinline__ void tsci_flush_global_nd(const DepArgs& a, uint32_t 
 // scan's segments stop at lanes 8, 16 and 24, so a run total covers at most 32
 // particles and the 12 outer entries stay below 32 * 2^26.6 < 2^32.
 __global__ void __launch_bounds__(DEP_THREADS, 4) deposit_runs_tsci(DepArgs a) {
+    if (gated_off(a)) return;
     const int lane = threadIdx.x & 31;
     const size_t gw = (size_t)blockIdx.x * DEP_WARPS + (threadIdx.x >> 5);
     const size_t stride = (size_t)gridDim.x * DEP_WARPS * 128;
@@ -878,6 +887,7 @@ __global__ void __launch_bounds__(DEP_THREADS, 4) deposit_runs_tsci(DepArgs a) {
 // registers (4 CTAs per SM, a few spilled words): latency-bound, it measured 7 %
 // faster per 2048^2 time step than with 80 registers and 3 CTAs.
 __global__ void __launch_bounds__(DEP_THREADS, 4) deposit_runs_tsc(DepArgs a) {
+    if (gated_off(a)) return;
     const int lane = threadIdx.x & 31;
     const size_t gw = (size_t)blockIdx.x * DEP_WARPS + (threadIdx.x >> 5);
     const size_t stride = (size_t)gridDim.x * DEP_WARPS * 128;
@@ -1196,6 +1206,7 @@ __host__ __device__ constexpr size_t cells_fixed_bytes() {
 
 template <int S, int LPP, int NW, int MINB, bool QC, bool KEYS, int NBUF>
 __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
+    if (gated_off(a)) return;
     constexpr int NX = Frame<S>::NX, LO = Frame<S>::LO, V = Frame<S>::V;
     constexpr int NV = NX * NX;
     constexpr int NF = StageFields<S, QC>::NF - (KEYS ? 0 : 1);  // the cell key is staged only with KEYS
@@ -1445,7 +1456,10 @@ __global__ void __launch_bounds__(NW * 32, MINB) deposit_cells(DepArgs a) {
     }
     cp_async_wait<0>();
     if constexpr (KEYS) {
-        if (lane == 0 && moved) atomicAdd(&a.st->moved, (unsigned long long)moved);
+        if (lane == 0 && moved) {
+            atomicAdd(&a.st->moved, (unsigned long long)moved);
+            atomicAdd(&a.st->moved_dep, (unsigned long long)moved);
+        }
     }
     __syncthreads();
     if (dense) return;
@@ -1495,9 +1509,69 @@ static int launch_cells(pic_ctx* c, const DepArgs& a, unsigned tiles) {
     return PIC_OK;
 }
 
+// After a deposit between sorts whose kernel was chosen on the device: once the
+// cell kernel has found more than `limit` particles outside their sorted cell,
+// the any-order kernel takes the following deposits (it is faster when most
+// particles have moved: every mover is a separate frame of atomics in the cell
+// kernel) until the next sort clears the flag. A deposit made in any order
+// counts every particle as moved, so a sort triggered by the moved fraction
+// still follows.
+__global__ void choose_any_order(DevStats* st, unsigned long long limit, unsigned long long n) {
+    if (st->any_order)
+        st->moved += n;
+    else if (st->moved_dep > limit)
+        st->any_order = 1u;
+    st->moved_dep = 0;
+}
+
+// The fraction of the particles above which deposits between sorts switch to
+// the any-order kernel (measured crossover at 1024^2, TSC: the cell kernel takes
+// about 6.7 ms with every particle moved, the any-order kernel 3.0 ms).
+constexpr double ANY_ORDER_FRACTION = 0.4;
+
 template <int S>
-// kernel choice: 0 tiled (cell-sorted), 1 run-aggregating (any order), 2 one thread per particle
-static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
+static int launch_runs(pic_ctx* c, const DepArgs& a) {
+    int sms = 148;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    size_t blocks = (a.n + DEP_THREADS * 4 - 1) / (DEP_THREADS * 4);
+    const size_t cap = (size_t)sms * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks == 0) blocks = 1;
+    if constexpr (S == S_TSC) {
+        if (a.qc != 0.0f)
+            deposit_runs_tsci<<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
+        else
+            deposit_runs_tsc<<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
+    } else {
+        deposit_runs<S><<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
+    }
+    return check_launch(c, "deposit_runs");
+}
+
+template <int S>
+// kernel choice: 0 tiled (cell-sorted), 1 run-aggregating (any order), 2 one thread per particle;
+// `adaptive`: between sorts, the device picks the tiled or the any-order kernel (choose_any_order)
+static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind, bool adaptive) {
+    if (kind == 0 && adaptive && !c->sorted) {
+        DepArgs ak = a, ar = a;
+        ak.gate = ar.gate = &c->dstats->any_order;
+        ak.gate_when = 0;
+        ar.gate_when = 1;
+        const unsigned tiles = (unsigned)(a.tiles_x * ((c->Ny + a.tile_h - 1) / a.tile_h));
+        prof_begin(c, "deposit");
+        int rc = a.qc != 0.0f ? launch_cells<S, CELLS_LPP, 4, 4, true, true>(c, ak, tiles)
+                              : launch_cells<S, CELLS_LPP, 4, 4, false, true>(c, ak, tiles);
+        if (rc == PIC_OK) rc = check_launch(c, "deposit_cells");
+        if (rc == PIC_OK) rc = launch_runs<S>(c, ar);
+        if (rc == PIC_OK) {
+            choose_any_order<<<1, 1, 0, c->stream>>>(c->dstats,
+                                                     (unsigned long long)(ANY_ORDER_FRACTION * (double)a.n),
+                                                     (unsigned long long)a.n);
+            rc = check_launch(c, "choose_any_order");
+        }
+        prof_end(c);
+        return rc;
+    }
     if (kind == 0) {
         const unsigned tiles = (unsigned)(a.tiles_x * ((c->Ny + a.tile_h - 1) / a.tile_h));
         prof_begin(c, "deposit");
@@ -1519,24 +1593,14 @@ static int launch_deposit(pic_ctx* c, const DepArgs& a, int kind) {
         if (rc != PIC_OK) return rc;
         return check_launch(c, "deposit_cells");
     }
+    if (kind == 1) {
+        prof_begin(c, "deposit");
+        const int rc = launch_runs<S>(c, a);
+        prof_end(c);
+        return rc;
+    }
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    if (kind == 1) {
-        size_t blocks = (a.n + DEP_THREADS * 4 - 1) / (DEP_THREADS * 4);
-        const size_t cap = (size_t)sms * 8;
-        if (blocks > cap) blocks = cap;
-        if (blocks == 0) blocks = 1;
-        prof_begin(c, "deposit");
-        if constexpr (S == S_TSC) {
-            if (a.qc != 0.0f)
-                deposit_runs_tsci<<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
-            else
-                deposit_runs_tsc<<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
-        } else
-            deposit_runs<S><<<(unsigned)blocks, DEP_THREADS, 0, c->stream>>>(a);
-        prof_end(c);
-        return check_launch(c, "deposit_runs");
-    }
     size_t blocks = (a.n + DEP_THREADS - 1) / DEP_THREADS;
     const size_t cap = (size_t)sms * 16;
     if (blocks > cap) blocks = cap;
@@ -1595,19 +1659,22 @@ int deposit_rho(pic_ctx* c, int scheme, double dt, double background) {
     a.tiles_x = (c->Nx + c->tile_w - 1) / c->tile_w;
     a.qc = c->qn_uniform;
     a.st = c->dstats;
+    a.gate = nullptr;
+    a.gate_when = 0;
+    const bool adaptive = c->order_mode == PIC_ORDER_AUTO;
     if (c->n > 0) {
         switch (scheme) {
             case PIC_SCHEME_NGP:
-                PIC_TRY(launch_deposit<S_NGP>(c, a, tiled));
+                PIC_TRY(launch_deposit<S_NGP>(c, a, tiled, adaptive));
                 break;
             case PIC_SCHEME_CIC:
-                PIC_TRY(launch_deposit<S_CIC>(c, a, tiled));
+                PIC_TRY(launch_deposit<S_CIC>(c, a, tiled, adaptive));
                 break;
             case PIC_SCHEME_TSC:
-                PIC_TRY(launch_deposit<S_TSC>(c, a, tiled));
+                PIC_TRY(launch_deposit<S_TSC>(c, a, tiled, adaptive));
                 break;
             default:
-                PIC_TRY(launch_deposit<S_ESK>(c, a, tiled));
+                PIC_TRY(launch_deposit<S_ESK>(c, a, tiled, adaptive));
                 break;
         }
     }

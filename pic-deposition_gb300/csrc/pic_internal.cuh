@@ -25,7 +25,9 @@ struct DevStats {
     unsigned int q_mixed;       // uploads: nonzero when the stored charges differ
     float q_first;              // uploads: the first particle's stored charge
     float q_raw0;               // uploads: the first particle's charge before normalisation
+    unsigned int any_order;     // between sorts: 1 once most particles have left their sorted cell
     unsigned long long moved;   // deposits between sorts: particles found outside their sorted cell
+    unsigned long long moved_dep;  // the same, for the any_order decision after each deposit
 };
 
 enum DevErr : int {

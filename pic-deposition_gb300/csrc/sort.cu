@@ -397,6 +397,8 @@ int sort_particles(pic_ctx* c, bool perm) {
         for (int j = 0; j < nf; ++j) std::swap(*slots[fields[j]], c->alt[fields[j]]);
     }
     PIC_TRY(build_offsets(c, c->cell));
+    // deposits between the sorts start again with the cell kernel
+    PIC_CUDA_TRY(cudaMemsetAsync(&c->dstats->any_order, 0, sizeof(unsigned int), c->stream));
     c->sorted = 1;
     c->part_valid = 1;
     return PIC_OK;

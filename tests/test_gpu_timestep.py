@@ -138,6 +138,31 @@ def test_sort_by_moved_fraction(pg, port):
     assert sorts[(8, 0.6)] >= 30 // 8
 
 
+@pytest.mark.parametrize("scheme", [CIC, TSC])
+def test_hot_plasma_switches_to_any_order_between_sorts(pg, port, scheme):
+    """Particles fast enough (about 0.7 cells per step and axis) that most leave
+    their cell every step: after the first deposit between sorts
+    finds most of them out of their cell, the following deposits take the
+    any-order kernel (a choice made on the device) until the next sort. The run
+    gives the particles and the energy history of the run that sorts every step
+    bit for bit (kinetic energy to 1e-13), with and without graphs."""
+    nx = ny = 64
+    p = port.init_particles(0, nx, ny, 1.0, 1.0, 40000, p0=8.0, seed=5)
+    outs = []
+    for k, graph in ((1, False), (10, True), (10, False)):
+        with start(pg, nx, ny, 1.0, 1.0, p) as c:
+            h = c.run(25, scheme=scheme, dt=0.004, sort_interval=k, use_graph=graph)
+            lay = c.device_layout()
+        key = np.lexsort((lay["vy"], lay["vx"], lay["yr"], lay["xr"], lay["cell"]))
+        outs.append((h, {kk: v[key] for kk, v in lay.items()}))
+    for h, lay in outs[1:]:
+        for kk in lay:
+            assert np.array_equal(lay[kk], outs[0][1][kk])
+        for col in (0, 1, 2, 4):
+            assert np.array_equal(h[:, col], outs[0][0][:, col])
+        assert np.allclose(h[:, 3], outs[0][0][:, 3], rtol=1e-13, atol=0)
+
+
 def test_rbgs_matches_oracle(pg, port):
     nx, ny = 64, 48
     rng = np.random.default_rng(0)
