@@ -60,7 +60,12 @@ extern "C" {
 #define PIC_SCHEME_ESIRKEPOV 3 /* the reference's trajectory-averaged rho (ngp.cpp:13-84) */
 
 /* ---- deposit ordering modes ---- */
-#define PIC_ORDER_AUTO 0     /* tiled kernel when cell-sorted, else the run-aggregating kernel   */
+/* PIC_ORDER_AUTO: the tiled kernel when cell-sorted; between sorts (particles
+ * pushed since) the tiled kernel that also finds the particles that left their
+ * cell, until one deposit finds more than 40 % of them moved, then the
+ * run-aggregating kernel until the next sort (chosen on the device); otherwise
+ * the run-aggregating kernel. Every choice gives the same grid bit for bit. */
+#define PIC_ORDER_AUTO 0
 #define PIC_ORDER_SORTED 1   /* tiled kernel; PIC_ERR_STATE unless sorted (or only pushed since) */
 #define PIC_ORDER_UNSORTED 2 /* run-aggregating kernel (any order; fast when nearly sorted)      */
 #define PIC_ORDER_ATOMIC 3   /* one thread per particle, one int64 atomic per stencil node       */
