@@ -50,7 +50,7 @@ extern "C" {
 #define PIC_ERR_OVERFLOW (-5)    /* fixed-point headroom would be exceeded              */
 #define PIC_ERR_COURANT (-6)     /* Esirkepov current needs |v|*dt < cell size          */
 #define PIC_ERR_TIMEOUT (-7)     /* a bounded device-side wait gave up                  */
-#define PIC_ERR_UNSUPPORTED (-8) /* valid request this build does not support           */
+#define PIC_ERR_UNSUPPORTED (-8) /* valid request the library does not support         */
 #define PIC_ERR_DEVICE (-9)      /* a kernel reported bad data (non-finite position ...) */
 
 /* ---- schemes: values of pic::DepositionScheme (src/deposition/deposition.hpp:11) ---- */
