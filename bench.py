@@ -567,7 +567,9 @@ def run_gpu(args, d: Dist):
     t0 = time.perf_counter()
     ctx.run(20, scheme=SCHEMES["TSC"], dt=ESK_DT, background=float(PPC), sort_interval=10, use_graph=True)
     extras["timestep_tsc_sort10"] = {"ms_per_step": (time.perf_counter() - t0) * 1e3 / 20,
-                                     "particles_per_s": n * 20 / (time.perf_counter() - t0)}
+                                     "particles_per_s": n * 20 / (time.perf_counter() - t0),
+                                     "setup": "the headline particles, charge -1 each with a background of 64 per "
+                                              "cell: a hot plasma, most particles change cell every step"}
     # the general path: per-particle charges (alternating +-1) are read as a charge stream
     ctx.upload(p["x"], p["y"], np.where(np.arange(n) % 2 == 0, 1.0, -1.0), p["vx"], p["vy"], p["m"])
     ctx.sort()
